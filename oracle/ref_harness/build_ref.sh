@@ -1,0 +1,28 @@
+#!/usr/bin/env bash
+# Builds the reference-side test harnesses from the read-only reference tree,
+# in place, with outputs only under oracle/_ref/. Needs the reference checkout
+# (RISA_REF_ROOT, default /root/reference); prints a note and exits 0 without it.
+#   librisa_ref_host.so : the reference's host-side table builders (CPU only)
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${RISA_REF_ROOT:-/root/reference}"
+OUT="$HERE/../_ref"
+if [ ! -d "$REF/RISA/risaLib/src" ]; then
+  echo "build_ref: reference tree not found at $REF; skipping"; exit 0
+fi
+mkdir -p "$OUT"
+NVCC="${NVCC:-nvcc}"
+INC=(-I"$HERE" -I"$HERE/stubs" -I"$REF/RISA/risaLib/src" -I"$REF/RISA/risaLib/include"
+     -I"$REF/RISA/glados/include")
+FLAGS=(-std=c++17 -O2 -Xcompiler -fPIC -Xcompiler -ffp-contract=off
+       -include "$HERE/stubs/risa_ref_preinclude.h" -w -diag-suppress 20012,550,177)
+pids=()
+for tu in ref_host_fan2para ref_host_attenuation ref_host_filter; do
+  "$NVCC" "${FLAGS[@]}" "${INC[@]}" -c "$HERE/$tu.cu" -o "$OUT/$tu.o" & pids+=($!)
+done
+# The stages' readConfig paths reference ConfigReader's constructor.
+"$NVCC" "${FLAGS[@]}" "${INC[@]}" -x cu -c "$REF/RISA/risaLib/src/ConfigReader/ConfigReader.cpp" \
+  -o "$OUT/ref_host_configreader.o" & pids+=($!)
+for p in "${pids[@]}"; do wait "$p"; done
+"$NVCC" -shared -o "$OUT/librisa_ref_host.so" "$OUT"/ref_host_*.o -lcufft -lgomp
+echo "build_ref: wrote $OUT/librisa_ref_host.so"
