@@ -1,0 +1,415 @@
+"""Benchmark of the streaming FBP chain on the full-rate streaming workload.
+
+Workload (one step): 2 detector planes x 2000 frames = 4000 slices of
+1000 fan projections x 1152 detectors (uint16, Poisson counts, 1% seeded
+defective detector columns) -> defect repair -> attenuation -> rebinning to
+1024 angles x 1024 rays -> Shepp-Logan filter (zero padded to 2048) ->
+backprojection to 512 x 512 FP32 images with the circular mask.
+
+  value  slices/s of the whole job with the raw frames resident in HBM, the job
+         replayed as one captured CUDA graph (batched path)
+  e2e    slices/s through the host-buffer entry point risa_gb_fbp_run_host:
+         pinned host frames in, pinned host images out, copies overlapped with
+         compute, all inside the timed region
+  plain  slices/s of the per-stage path (one frame per launch, a stream sync
+         after every stage, as the reference's stage threads do)
+
+`python bench.py --impl reference` times the FP64 CPU oracle FBP on the host
+cores instead (the reference has no CPU implementation of the chain).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(n_planes=2, n_fan_det=1152, n_fan_proj=1000, n_par_proj=1024, n_par_det=1024, n_pixels=512,
+                source_offset=0.0, detector_diameter=480.0, image_width=200.0, source_diameter=[430.0, 430.0],
+                delta_x=[0.0, 0.0], delta_z=[1417.0, 1430.0], source_angle=[360.0, 360.0])
+FRAMES_PER_PLANE = 2000
+FLOPS_PER_UPDATE = 6  # ray coordinate FMA (2) + weight add (1) + interpolation FMA (2) + accumulate (1)
+WORKLOAD_NAME = ("full-rate streaming: 2 planes x 2000 frames of 1000x1152 uint16 fan sinograms, 1% defective "
+                 "detectors -> 1024x1024 parallel (pad 2048, Shepp-Logan) -> 512^2 FP32, circular mask")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--frames", type=int, default=FRAMES_PER_PLANE, help="frames per plane")
+    ap.add_argument("--batch", type=int, default=64, help="frames per engine chunk (multiple of 2)")
+    ap.add_argument("--distinct", type=int, default=8, help="distinct synthetic frames per plane")
+    ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/roofline/cpu legs")
+    return ap.parse_args()
+
+
+def make_oracle_geom():
+    class G:
+        pass
+
+    g = G()
+    g.__dict__.update(WORKLOAD, image_center_x=0.0, image_center_y=0.0, rotation_offset=0.0)
+    return g
+
+
+def synthetic_scan(frames_per_plane: int, distinct: int):
+    from risa_gb300 import phantom
+
+    w = WORKLOAD
+    return phantom.make_scan(frames_per_plane, w["n_planes"], w["n_fan_proj"], w["n_fan_det"],
+                             w["source_diameter"][0] / 2.0, w["detector_diameter"] / 2.0, seed=2026,
+                             defect_fraction=0.01, distinct=distinct)
+
+
+def oracle_fbp_sample(sc, n_slices: int, threads: int):
+    """FP64 CPU oracle on the first n_slices frames; returns (images, seconds)."""
+    import oracle
+
+    og = make_oracle_geom()
+    op = oracle.make_params(quirk=oracle.QUIRK_NONE, filter_type="sheppLogan", defects=True, masking=True)
+    ref, dark = oracle.attenuation_init(sc.ref, sc.dark, WORKLOAD["n_planes"], 0.67, 1.5, True, oracle.QUIRK_NONE)
+    rec = oracle.f2p_records(og, oracle.QUIRK_NONE)
+    t0 = time.perf_counter()
+    out = oracle.fbp(og, op, rec, ref, dark, sc.raw[:n_slices], sc.planes[:n_slices], n_threads=threads)
+    return out, time.perf_counter() - t0, (ref, dark, rec, op, og)
+
+
+# --------------------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.path or not os.path.exists(self.path):
+            return None
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        power = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(power) if power else None}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+# --------------------------------------------------------------------------- reference arm
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    sc = synthetic_scan(max(1, cores // 2 + 1), 2)
+    n = min(sc.raw.shape[0], max(2, cores))
+    times = []
+    for i in range(args.warmup + args.steps):
+        _, dt, _ = oracle_fbp_sample(sc, n, cores)
+        if i >= args.warmup:
+            times.append(dt)
+    sec = sum(times) / len(times)
+    value = n / sec
+    line = {
+        "impl": "reference", "metric": "FBP slices/s @512^2", "value": value, "unit": "slices/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD_NAME, "sample_slices_per_step": n},
+        "cpu_baseline": {"value": value, "unit": "slices/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} slices of the workload per step (FP64 C oracle, {cores} threads)"},
+        "e2e": {"value": value, "unit": "slices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- our arm
+def run_ours(args, rank: int, world: int, local_rank: int):
+    import torch
+    import torch.distributed as dist
+
+    import risa_gb300 as rg
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    L = WORKLOAD["n_planes"]
+    B = args.batch - args.batch % L
+    g = rg.make_geometry(**WORKLOAD)
+    p = rg.make_params(filter_type="sheppLogan", defects=True, masking=True)
+    sc = synthetic_scan(args.frames, args.distinct)
+    n = sc.raw.shape[0]
+    Pf, Df, N = WORKLOAD["n_fan_proj"], WORKLOAD["n_fan_det"], WORKLOAD["n_pixels"]
+    Pp, Dp = WORKLOAD["n_par_proj"], WORKLOAD["n_par_det"]
+    fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=B)
+    raw = torch.from_numpy(sc.raw.view(np.int16)).to(dev)
+    img = torch.empty((n, N, N), dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    # autotune the backprojection tile shape on this geometry, then capture the job
+    fan_buf, par_buf = fbp.intermediates()
+    with torch.cuda.stream(stream):
+        fbp.enqueue(raw[:B], img[:B], rg.PLANES_INTERLEAVED, B, stream)
+    stream.synchronize()
+    bp = fbp.backprojection()
+    variant = bp.autotune(par_buf, img.data_ptr(), B, stream)
+    graph = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, stream)
+    launches_per_step = graph.kernel_count
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        graph.replay(stream)
+    stream.synchronize()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(local_rank) as clk:
+        torch.cuda.synchronize()
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            graph.replay(stream)
+        e1.record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms / 1e3)
+    clocks = clk.summary()
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras = measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
+    if rank != 0:
+        return
+    peaks = measured_peaks()
+    line = {
+        "metric": "FBP slices/s @512^2", "value": value, "unit": "slices/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ellipse phantoms, Poisson uint16 counts; "
+                f"{args.distinct} distinct frames per plane cycled)",
+        "config": {"workload": WORKLOAD_NAME, "frames_per_plane": args.frames, "slices_per_step": n,
+                   "batch": B, "bp_variant": variant, "graph": "one CUDA graph per step",
+                   "l2": "inputs larger than L2 (%.1f GB raw per step)" % (sc.raw.nbytes / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+    }
+    line.update(extras)
+    if "plain" in line:
+        line["speedup_vs_plain"] = value / world / line["plain"]["value"]
+    if "roofline" in line and peaks:
+        line["roofline"]["peaks_file"] = {k: peaks.get(k) for k in ("hbm_gbs", "sm_max_mhz")}
+    print(json.dumps(line), flush=True)
+
+
+def timed(torch, stream, fn, reps: int) -> float:
+    """Average ms of fn() on `stream` over reps, after one warm-up call."""
+    fn()
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p):
+    out = {}
+    dev = raw.device
+    n = sc.raw.shape[0]
+    L = WORKLOAD["n_planes"]
+    Pf, Df, N = WORKLOAD["n_fan_proj"], WORKLOAD["n_fan_det"], WORKLOAD["n_pixels"]
+    Pp, Dp = WORKLOAD["n_par_proj"], WORKLOAD["n_par_det"]
+    peaks = measured_peaks()
+    props = torch.cuda.get_device_properties(dev)
+    sms = props.multi_processor_count
+    sm_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 2.0 * 128 * sms * sm_mhz * 1e6 / 1e12  # TFLOP/s
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+
+    # ---- per-stage timings on one chunk (isolated kernels, CUDA events on the launch stream)
+    fan_buf, par_buf = fbp.intermediates()
+    att = rg.Attenuation(g, p, sc.ref, 1, sc.dark, 1)
+    f2p = rg.Fan2Para(g, p)
+    filt = rg.Filter(g, p)
+    bp = fbp.backprojection()
+    reps = 5
+    t_att = timed(torch, stream, lambda: att.enqueue(raw[:B], fan_buf, rg.PLANES_INTERLEAVED, B, stream), reps)
+    t_f2p = timed(torch, stream, lambda: f2p.enqueue(fan_buf, par_buf, rg.PLANES_INTERLEAVED, B, stream), reps)
+    par_copy = torch.randn((B, Pp, Dp), dtype=torch.float32, device=dev)
+    t_filt = timed(torch, stream, lambda: filt.enqueue(par_copy, B, stream), reps)
+    t_bp = timed(torch, stream, lambda: bp.enqueue(par_buf, img[:B], B, stream), reps)
+    fs, ps = Pf * Df, Pp * Dp
+    att_bytes = B * fs * (2 + 4) + L * fs * 4
+    f2p_bytes = B * (fs * 4 + ps * 4) + L * ps * 4 * 12
+    filt_bytes = B * ps * 8
+    yy, xx = np.mgrid[:N, :N]
+    inside = int(((xx - (N - 1) / 2) ** 2 + (yy - (N - 1) / 2) ** 2 <= N * N / 4).sum())
+    updates = B * inside * Pp
+    bp_tflops = updates * FLOPS_PER_UPDATE / (t_bp / 1e3) / 1e12
+    out["roofline"] = {
+        "kernel": "bp_tile (backprojection)", "bound": "fp32", "achieved": bp_tflops, "peak": fp32_peak,
+        "unit": "TFLOP/s", "frac": bp_tflops / fp32_peak, "traffic": None,
+        "work": f"{FLOPS_PER_UPDATE} FLOP per pixel x angle update, {inside} in-circle pixels x {Pp} angles "
+                f"x {B} slices per launch",
+        "peak_source": f"nominal FFMA rate: 128 lanes x 2 FLOP x {sms} SMs x {sm_mhz:.0f} MHz "
+                       "(MEASURED_PEAKS.json carries no FP32 figure)",
+    }
+    out["bp"] = {"gupdates_per_s": updates / (t_bp / 1e3) / 1e9,
+                 "gupdates_per_s_full_square": B * N * N * Pp / (t_bp / 1e3) / 1e9,
+                 "ms_per_launch": t_bp, "slices_per_launch": B}
+    out["stages"] = {
+        "attenuation_defects": {"ms": t_att, "gbs": att_bytes / (t_att / 1e3) / 1e9,
+                                "frac_hbm": att_bytes / (t_att / 1e3) / 1e9 / hbm},
+        "fan2para": {"ms": t_f2p, "gbs": f2p_bytes / (t_f2p / 1e3) / 1e9,
+                     "frac_hbm": f2p_bytes / (t_f2p / 1e3) / 1e9 / hbm},
+        "filter": {"ms": t_filt, "gbs": filt_bytes / (t_filt / 1e3) / 1e9,
+                   "frac_hbm": filt_bytes / (t_filt / 1e3) / 1e9 / hbm},
+        "backprojection": {"ms": t_bp},
+        "hbm_peak_gbs": hbm, "batch": B,
+    }
+
+    # ---- plain per-stage path: one frame per launch, sync after every stage
+    dfx = rg.Defects(g, p, max_batch=1)
+    ws = torch.empty(dfx.workspace_bytes(1), dtype=torch.uint8, device=dev)
+    raw1 = torch.empty((1, Pf, Df), dtype=torch.int16, device=dev)
+    n_plain = min(64, n)
+
+    def plain():
+        for f in range(n_plain):
+            k = f % L
+            raw1.copy_(raw[f:f + 1])
+            dfx.enqueue(raw1, 1, ws, stream=stream)
+            stream.synchronize()
+            att.enqueue(raw1, fan_buf, k, 1, stream)
+            stream.synchronize()
+            f2p.enqueue(fan_buf, par_buf, k, 1, stream)
+            stream.synchronize()
+            filt.enqueue(par_buf, 1, stream)
+            stream.synchronize()
+            bp.enqueue(par_buf, img[f:f + 1], 1, stream)
+            stream.synchronize()
+
+    with torch.cuda.stream(stream):
+        plain()
+        t0 = time.perf_counter()
+        plain()
+        t_plain = time.perf_counter() - t0
+    plain_value = n_plain / t_plain
+    out["plain"] = {"value": plain_value, "unit": "slices/s", "frames": n_plain,
+                    "how": "one frame per stage launch, stream sync after each stage, device-resident input"}
+
+    # ---- end to end through the host-buffer entry point
+    hraw = torch.from_numpy(sc.raw.view(np.int16)).pin_memory()
+    himg = torch.empty((n, N, N), dtype=torch.float32).pin_memory()
+    fbp.run_host(hraw, himg, n, rg.PLANES_INTERLEAVED)  # warm-up (captures the slot graphs)
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        fbp.run_host(hraw, himg, n, rg.PLANES_INTERLEAVED)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    out["e2e"] = {"value": n / t_e2e, "unit": "slices/s", "h2d_bytes_per_step": int(sc.raw.nbytes),
+                  "d2h_bytes_per_step": int(n * N * N * 4), "entry_point": "risa_gb_fbp_run_host"}
+
+    # ---- accuracy of the batched output against the FP64 oracle, and the CPU baseline
+    cores = os.cpu_count() or 1
+    n_cpu = min(n, max(4, cores))
+    ref_imgs, sec, _ = oracle_fbp_sample(sc, n_cpu, cores)
+    fbp.enqueue(raw[:B], img[:B], rg.PLANES_INTERLEAVED, B, stream)
+    stream.synchronize()
+    got = img[:n_cpu].cpu().numpy().astype(np.float64)
+    d = got - ref_imgs
+    out["accuracy"] = {
+        "slices": n_cpu,
+        "rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref_imgs)),
+        "max_rel": float(np.abs(d).max() / np.abs(ref_imgs).max()),
+        "vs": "FP64 CPU oracle on the same inputs",
+    }
+    out["cpu_baseline"] = {"value": n_cpu / sec, "unit": "slices/s", "cores": cores, "kind": "port",
+                           "sample": f"{n_cpu} slices of the workload, FP64 C oracle, {cores} threads"}
+    return out
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,276 @@
+/*
+ * risa_gb300.h -- C ABI of the GB300-native streaming FBP chain.
+ *
+ * One entry-point family per stage of the reference's reconstruction chain.
+ * The reference exposes these stages as C++ classes driven by its GLADOS
+ * pipeline: a config-file constructor, process(Image&&) and wait() -> Image,
+ * with one CUDA stream and one processor thread per device. Here each stage is
+ *   risa_gb_<stage>_create(geometry, params, ..., &handle)  -- init work, tables
+ *   risa_gb_<stage>_enqueue(handle, device in/out pointers, batch, stream)
+ *   risa_gb_<stage>_destroy(handle)
+ * and the C++ stage classes in risa_gb300/cpp wrap these calls to keep the
+ * reference's process()/wait() contract.
+ *
+ * Conventions
+ *   - Every function returns a risa_gb_status (0 = success, < 0 = error);
+ *     risa_gb_last_error() gives a thread-local description.
+ *   - Device pointers are caller-owned. Enqueue calls are stream-ordered, do
+ *     not synchronise and do not allocate; tables are built at create time.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - Frames are row-major: fan sinogram [n_fan_proj][n_fan_det] (uint16 raw,
+ *     float attenuation), parallel sinogram [n_par_proj][n_par_det] float,
+ *     image [n_pixels][n_pixels] float. A batch is `batch` consecutive frames.
+ *   - Plane selection: plane >= 0 -> every frame of the batch belongs to that
+ *     plane; RISA_GB_PLANES_INTERLEAVED -> frame b belongs to plane
+ *     b % n_planes (the order in which a multi-plane scan arrives).
+ */
+#ifndef RISA_GB300_H
+#define RISA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int risa_gb_status;
+#define RISA_GB_OK 0
+#define RISA_GB_EINVAL (-1)       /* bad argument */
+#define RISA_GB_EUNSUPPORTED (-2) /* shape or option this build does not support */
+#define RISA_GB_ECUDA (-3)        /* a CUDA runtime call failed */
+#define RISA_GB_ETIMEDOUT (-4)    /* a bounded device-side wait ran out */
+#define RISA_GB_ENOMEM (-5)       /* device or host allocation failed at create time */
+#define RISA_GB_ECONFIG (-6)      /* configuration file missing or malformed */
+
+#define RISA_GB_MAX_PLANES 4
+#define RISA_GB_PLANES_INTERLEAVED (-1)
+
+/* Quirk modes. RISA reproduces the reference's index behaviour bit for bit
+ * (zeroed dark average, (frame + plane) reference indexing, unsigned modulo
+ * wraps in the defect search, alpha[0] = 0, stale ray-2 theta search,
+ * unpadded circular filter, detector-edge backprojection convention). NONE is
+ * the physically corrected chain used for the benchmark configurations. */
+#define RISA_GB_QUIRKS_NONE 0
+#define RISA_GB_QUIRKS_RISA 1
+
+/* Filter types (the reference's detail::FilterType order, Filter.h:47-53). */
+#define RISA_GB_FILTER_RAMP 0
+#define RISA_GB_FILTER_SHEPP_LOGAN 1
+#define RISA_GB_FILTER_COSINE 2
+#define RISA_GB_FILTER_HAMMING 3
+#define RISA_GB_FILTER_HANNING 4
+
+/* Backprojection interpolation (Backprojection.cu:238-336). */
+#define RISA_GB_INTERP_LINEAR 0
+#define RISA_GB_INTERP_NEAREST 1
+#define RISA_GB_INTERP_NEAREST_TRUNC 2 /* the reference's texture variant */
+
+/* Scan geometry: the keys of the reference's config file (config.cfg:29-56). */
+typedef struct risa_gb_geometry {
+   uint32_t struct_size;     /* sizeof(risa_gb_geometry) */
+   int32_t n_planes;         /* numberOfPlanes */
+   int32_t n_fan_det;        /* numberOfFanDetectors */
+   int32_t n_fan_proj;       /* samplingRate*1e6/scanRate */
+   int32_t n_par_proj;       /* numberOfParallelProjections (over 180 degrees) */
+   int32_t n_par_det;        /* numberOfParallelDetectors */
+   int32_t n_pixels;         /* numberOfPixels */
+   int32_t n_modules;        /* numberOfDetectorModules (raw module-major layout) */
+   double source_offset;     /* sourceOffset, degrees */
+   double detector_diameter; /* detectorDiameter, mm */
+   double image_width;       /* imageWidth, mm */
+   double image_center_x;    /* imageCenterX, mm */
+   double image_center_y;    /* imageCenterY, mm */
+   double rotation_offset;   /* rotationOffset, degrees */
+   double source_diameter[RISA_GB_MAX_PLANES]; /* sourceDiameter[plane], mm */
+   double delta_x[RISA_GB_MAX_PLANES];         /* deltaX[plane] */
+   double delta_z[RISA_GB_MAX_PLANES];         /* deltaZ[plane] */
+   double source_angle[RISA_GB_MAX_PLANES];    /* sourceAngle[plane], degrees */
+} risa_gb_geometry;
+
+/* Processing options (the remaining config keys, plus this build's own). */
+typedef struct risa_gb_params {
+   uint32_t struct_size;     /* sizeof(risa_gb_params) */
+   int32_t quirks;           /* RISA_GB_QUIRKS_* */
+   int32_t filter_type;      /* filterType */
+   double cutoff;            /* cutoffFraction */
+   int32_t pad;              /* FFT length; 0 = next power of two >= 2*n_par_det (NONE mode) */
+   int32_t interp;           /* interpolationType */
+   int32_t defects;          /* run detector-defect repair on every frame */
+   double thresh_min;        /* thresh_min */
+   double thresh_max;        /* thresh_max */
+   int32_t relevant_mask;    /* apply the ROFEX relevant-area mask in attenuation */
+   double lower_lim_offset;  /* lowerLimOffset */
+   double upper_lim_offset;  /* upperLimOffset */
+   uint32_t xa, xb, xc, xd, xe, xf; /* relevant-area fix points */
+   int32_t masking;          /* circular image mask */
+   double masking_value;     /* maskingValue */
+   int32_t normalize;        /* min-max normalisation before masking */
+   int32_t repair_reference; /* repair defects in reference frames at init */
+} risa_gb_params;
+
+/* Fill defaults (ramp, cutoff 1, auto pad, linear, NONE quirks, thresholds
+ * 0.67/1.5 as the reference's ROFEX III setting, no masks). */
+risa_gb_status risa_gb_params_init(risa_gb_params* p);
+risa_gb_status risa_gb_geometry_init(risa_gb_geometry* g);
+
+const char* risa_gb_last_error(void);
+const char* risa_gb_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Config files: the reference's libconfig format (RISA/example/config.cfg),
+ * parsed by this library (key = value; lists in [ ]). Replaces the
+ * ConfigReader + readConfig pair of every stage (ConfigReader.h:62-86). */
+risa_gb_status risa_gb_config_load(const char* path, risa_gb_geometry* g, risa_gb_params* p);
+
+/* ---------------------------------------------------------------------------
+ * DetectorInterpolation (DetectorInterpolation.cu:105-140; algorithm
+ * interpolationFunctions.h:28-97). Finds defect or flickering detector
+ * columns per frame and repairs them in place, on the device. */
+typedef struct risa_gb_defects risa_gb_defects;
+risa_gb_status risa_gb_defects_create(const risa_gb_geometry* g, const risa_gb_params* p,
+                                      int max_batch, risa_gb_defects** out);
+/* Bytes of device workspace an enqueue of `batch` frames needs. */
+size_t risa_gb_defects_workspace_bytes(const risa_gb_defects* h, int batch);
+/* frames: [batch][n_fan_proj][n_fan_det] uint16, repaired in place.
+ * flags_out: optional device int32 [batch][n_fan_det] receiving the defect flags. */
+risa_gb_status risa_gb_defects_enqueue(risa_gb_defects* h, uint16_t* frames, int batch,
+                                       int32_t* flags_out, void* workspace, void* stream);
+risa_gb_status risa_gb_defects_destroy(risa_gb_defects* h);
+
+/* ---------------------------------------------------------------------------
+ * Attenuation (Attenuation.cu:48-175, kernel :416-444). Create averages the
+ * reference and dark frames (after defect repair, Attenuation.cu:177-217) and
+ * builds the relevant-area mask (:327-381). ref_frames/dark_frames are host
+ * arrays [n_frames][n_planes][n_fan_proj][n_fan_det] uint16 (the reference's
+ * file order); dark may be NULL. */
+typedef struct risa_gb_attenuation risa_gb_attenuation;
+risa_gb_status risa_gb_attenuation_create(const risa_gb_geometry* g, const risa_gb_params* p,
+                                          const uint16_t* ref_frames, int n_ref,
+                                          const uint16_t* dark_frames, int n_dark,
+                                          risa_gb_attenuation** out);
+/* raw: [batch] uint16 fan frames -> out: [batch] float fan frames. */
+risa_gb_status risa_gb_attenuation_enqueue(risa_gb_attenuation* h, const uint16_t* raw,
+                                           float* out, int plane, int batch, void* stream);
+/* Device copies of the tables: ref average [L][P][D] float, dark [L][D] float. */
+risa_gb_status risa_gb_attenuation_tables(const risa_gb_attenuation* h, float* host_ref,
+                                          float* host_dark);
+risa_gb_status risa_gb_attenuation_destroy(risa_gb_attenuation* h);
+
+/* ---------------------------------------------------------------------------
+ * Fan2Para (Fan2Para.cu:44-249, tables :251-480, kernel
+ * cuda_kernels_fan2para.h:64-177). Rebins fan sinograms to 180-degree
+ * parallel sinograms through FP64-built gather tables. */
+typedef struct risa_gb_fan2para risa_gb_fan2para;
+risa_gb_status risa_gb_fan2para_create(const risa_gb_geometry* g, const risa_gb_params* p,
+                                       risa_gb_fan2para** out);
+/* fan: [batch][Pf][Df] float -> par: [batch][Pp][Dp] float. */
+risa_gb_status risa_gb_fan2para_enqueue(risa_gb_fan2para* h, const float* fan, float* par,
+                                        int plane, int batch, void* stream);
+/* Adjoint (transpose) of the rebinning: par [batch][Pp][Dp] -> fan [batch][Pf][Df]. */
+risa_gb_status risa_gb_fan2para_enqueue_adjoint(risa_gb_fan2para* h, const float* par,
+                                                float* fan, int plane, int batch,
+                                                void* stream);
+risa_gb_status risa_gb_fan2para_destroy(risa_gb_fan2para* h);
+
+/* Host-only table build (no GPU needed), for inspection and parity tests.
+ * For every output sample o in [Pp*Dp] of `plane` and slot r in 0..3 (slots
+ * 0,1: rays 1,2 of the sample itself; slots 2,3: rays 1,2 of its mirrored
+ * partner 180 degrees later): packed[r][o] = valid<<31 | theta_before<<16 |
+ * gamma_before, u[r][o], v[r][o]. Arrays hold 4*Pp*Dp entries. */
+risa_gb_status risa_gb_fan2para_tables_host(const risa_gb_geometry* g, const risa_gb_params* p,
+                                            int plane, uint32_t* packed, float* u, float* v);
+
+/* ---------------------------------------------------------------------------
+ * Filter (Filter.cu:102-191, applyFilter :231-241). Row-wise ramp-family
+ * filtering of parallel sinograms with this library's own FFT (no cuFFT),
+ * in place. */
+typedef struct risa_gb_filter risa_gb_filter;
+risa_gb_status risa_gb_filter_create(const risa_gb_geometry* g, const risa_gb_params* p,
+                                     risa_gb_filter** out);
+risa_gb_status risa_gb_filter_enqueue(risa_gb_filter* h, float* sino, int batch, void* stream);
+/* FFT length and the frequency response H[len/2+1] (host copy). */
+risa_gb_status risa_gb_filter_response(const risa_gb_filter* h, int* len, float* host_h);
+risa_gb_status risa_gb_filter_destroy(risa_gb_filter* h);
+/* Host-only filter design (no GPU). h: len/2 + 1 floats. */
+risa_gb_status risa_gb_filter_design_host(const risa_gb_geometry* g, const risa_gb_params* p,
+                                          int* len, float* h);
+
+/* ---------------------------------------------------------------------------
+ * Backprojection (Backprojection.cu:46-208, kernels :238-336) with the
+ * circular mask of Masking.cu:157-169 fused when masking is on and
+ * normalisation off. */
+typedef struct risa_gb_backprojection risa_gb_backprojection;
+risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* g, const risa_gb_params* p,
+                                             risa_gb_backprojection** out);
+/* sino: [batch][Pp][Dp] float -> img: [batch][N][N] float. */
+risa_gb_status risa_gb_backprojection_enqueue(risa_gb_backprojection* h, const float* sino,
+                                              float* img, int batch, void* stream);
+/* Adjoint: img [batch][N][N] -> sino [batch][Pp][Dp] (ray-driven forward projector,
+ * the exact transpose of the linear backprojection, without the mask). */
+risa_gb_status risa_gb_backprojection_enqueue_adjoint(risa_gb_backprojection* h,
+                                                      const float* img, float* sino,
+                                                      int batch, void* stream);
+/* Pick the fastest tile/angle-chunk variant for this geometry by timing the
+ * candidates on the device (uses the caller's buffers; result cached in the
+ * handle). variant_out may be NULL. */
+risa_gb_status risa_gb_backprojection_autotune(risa_gb_backprojection* h, const float* sino,
+                                               float* img, int batch, void* stream,
+                                               int* variant_out);
+risa_gb_status risa_gb_backprojection_set_variant(risa_gb_backprojection* h, int variant);
+int risa_gb_backprojection_variant_count(void);
+risa_gb_status risa_gb_backprojection_destroy(risa_gb_backprojection* h);
+
+/* ---------------------------------------------------------------------------
+ * Masking (Masking.cu:113-169): optional min-max normalisation, then the
+ * inscribed-circle mask, in place. */
+typedef struct risa_gb_masking risa_gb_masking;
+risa_gb_status risa_gb_masking_create(const risa_gb_geometry* g, const risa_gb_params* p,
+                                      risa_gb_masking** out);
+size_t risa_gb_masking_workspace_bytes(const risa_gb_masking* h, int batch);
+risa_gb_status risa_gb_masking_enqueue(risa_gb_masking* h, float* img, int batch,
+                                       void* workspace, void* stream);
+risa_gb_status risa_gb_masking_destroy(risa_gb_masking* h);
+
+/* ---------------------------------------------------------------------------
+ * Whole chain: raw uint16 fan frames -> masked images, batched. Holds every
+ * stage above plus its intermediate buffers (allocated at create time for
+ * max_batch frames). */
+typedef struct risa_gb_fbp risa_gb_fbp;
+risa_gb_status risa_gb_fbp_create(const risa_gb_geometry* g, const risa_gb_params* p,
+                                  const uint16_t* ref_frames, int n_ref,
+                                  const uint16_t* dark_frames, int n_dark, int max_batch,
+                                  risa_gb_fbp** out);
+/* raw [batch] device frames -> img [batch] device images; plane as above. */
+risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane,
+                                   int batch, void* stream);
+/* Capture the reconstruction of n_frames device frames (any count: processed
+ * in chunks of max_batch through the handle's buffers, chunk after chunk) as
+ * one CUDA graph with fixed device pointers. Replaying it reruns the whole
+ * job with a single launch. With interleaved planes, max_batch must be a
+ * multiple of n_planes. The graph uses the handle's buffers: do not replay it
+ * concurrently with other work on the same handle. */
+typedef struct risa_gb_graph risa_gb_graph;
+risa_gb_status risa_gb_fbp_graph_capture(risa_gb_fbp* h, const uint16_t* raw, float* img,
+                                         int plane, int n_frames, void* stream,
+                                         risa_gb_graph** out);
+risa_gb_status risa_gb_graph_replay(risa_gb_graph* g, void* stream);
+/* Number of kernel nodes in the captured graph. */
+int risa_gb_graph_kernel_count(const risa_gb_graph* g);
+risa_gb_status risa_gb_graph_destroy(risa_gb_graph* g);
+/* Host-buffer path, the H2D -> stages -> D2H flow of the reference's
+ * H2D/D2H stages (H2D.cu:134-169, D2H.cu:119-148): copies n_frames raw
+ * frames from host memory, reconstructs them in batches of the handle's
+ * max_batch with copies overlapped against compute on two streams, and
+ * copies the images back. Pinned host memory is fastest. Blocks until done. */
+risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, float* host_img,
+                                    int n_frames, int plane);
+/* Per-stage access for inspection (intermediate device buffers). */
+risa_gb_status risa_gb_fbp_intermediates(risa_gb_fbp* h, float** fan, float** par);
+risa_gb_backprojection* risa_gb_fbp_backprojection(risa_gb_fbp* h);
+risa_gb_status risa_gb_fbp_destroy(risa_gb_fbp* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,436 @@
+"""GB300-native streaming FBP chain (the reference's Attenuation -> DetectorInterpolation
+-> Fan2Para -> Filter -> Backprojection -> Masking stages), Python access to the C ABI.
+
+The compute lives in ``_build/librisa_gb300.so`` (sm_103a kernels behind the
+C ABI declared in ``include/risa_gb300.h``). This module only marshals
+geometry/parameter structs and device pointers (``int`` addresses or
+objects with ``data_ptr()``, e.g. torch tensors) through ctypes. There is no
+CPU fallback: if the library is missing, importing the stage classes fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "librisa_gb300.so")
+
+QUIRKS_NONE, QUIRKS_RISA = 0, 1
+FILTER_RAMP, FILTER_SHEPP_LOGAN, FILTER_COSINE, FILTER_HAMMING, FILTER_HANNING = range(5)
+FILTERS = {"ramp": 0, "sheppLogan": 1, "cosine": 2, "hamming": 3, "hanning": 4}
+INTERP_LINEAR, INTERP_NEAREST, INTERP_NEAREST_TRUNC = 0, 1, 2
+PLANES_INTERLEAVED = -1
+MAX_PLANES = 4
+
+STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported", -3: "CUDA error", -4: "timed out",
+          -5: "out of memory", -6: "configuration error"}
+
+
+class RisaError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str):
+        super().__init__(f"{what}: {STATUS.get(status, status)} ({detail})")
+        self.status = status
+
+
+class Geometry(ctypes.Structure):
+    """Mirror of risa_gb_geometry (config keys of the reference's config.cfg)."""
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32), ("n_planes", ctypes.c_int32), ("n_fan_det", ctypes.c_int32),
+        ("n_fan_proj", ctypes.c_int32), ("n_par_proj", ctypes.c_int32), ("n_par_det", ctypes.c_int32),
+        ("n_pixels", ctypes.c_int32), ("n_modules", ctypes.c_int32),
+        ("source_offset", ctypes.c_double), ("detector_diameter", ctypes.c_double),
+        ("image_width", ctypes.c_double), ("image_center_x", ctypes.c_double),
+        ("image_center_y", ctypes.c_double), ("rotation_offset", ctypes.c_double),
+        ("source_diameter", ctypes.c_double * MAX_PLANES), ("delta_x", ctypes.c_double * MAX_PLANES),
+        ("delta_z", ctypes.c_double * MAX_PLANES), ("source_angle", ctypes.c_double * MAX_PLANES),
+    ]
+
+
+class Params(ctypes.Structure):
+    """Mirror of risa_gb_params."""
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32), ("quirks", ctypes.c_int32), ("filter_type", ctypes.c_int32),
+        ("cutoff", ctypes.c_double), ("pad", ctypes.c_int32), ("interp", ctypes.c_int32),
+        ("defects", ctypes.c_int32), ("thresh_min", ctypes.c_double), ("thresh_max", ctypes.c_double),
+        ("relevant_mask", ctypes.c_int32), ("lower_lim_offset", ctypes.c_double),
+        ("upper_lim_offset", ctypes.c_double),
+        ("xa", ctypes.c_uint32), ("xb", ctypes.c_uint32), ("xc", ctypes.c_uint32),
+        ("xd", ctypes.c_uint32), ("xe", ctypes.c_uint32), ("xf", ctypes.c_uint32),
+        ("masking", ctypes.c_int32), ("masking_value", ctypes.c_double), ("normalize", ctypes.c_int32),
+        ("repair_reference", ctypes.c_int32),
+    ]
+
+
+# Every exported symbol of include/risa_gb300.h with its ctypes signature.
+_vp, _i, _sz, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_double
+_pp = ctypes.POINTER(ctypes.c_void_p)
+SIGNATURES = {
+    "risa_gb_params_init": (_i, [_vp]),
+    "risa_gb_geometry_init": (_i, [_vp]),
+    "risa_gb_last_error": (ctypes.c_char_p, []),
+    "risa_gb_version": (ctypes.c_char_p, []),
+    "risa_gb_config_load": (_i, [ctypes.c_char_p, _vp, _vp]),
+    "risa_gb_defects_create": (_i, [_vp, _vp, _i, _pp]),
+    "risa_gb_defects_workspace_bytes": (_sz, [_vp, _i]),
+    "risa_gb_defects_enqueue": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
+    "risa_gb_defects_destroy": (_i, [_vp]),
+    "risa_gb_attenuation_create": (_i, [_vp, _vp, _vp, _i, _vp, _i, _pp]),
+    "risa_gb_attenuation_enqueue": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
+    "risa_gb_attenuation_tables": (_i, [_vp, _vp, _vp]),
+    "risa_gb_attenuation_destroy": (_i, [_vp]),
+    "risa_gb_fan2para_create": (_i, [_vp, _vp, _pp]),
+    "risa_gb_fan2para_enqueue": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
+    "risa_gb_fan2para_enqueue_adjoint": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
+    "risa_gb_fan2para_destroy": (_i, [_vp]),
+    "risa_gb_fan2para_tables_host": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
+    "risa_gb_filter_create": (_i, [_vp, _vp, _pp]),
+    "risa_gb_filter_enqueue": (_i, [_vp, _vp, _i, _vp]),
+    "risa_gb_filter_response": (_i, [_vp, ctypes.POINTER(ctypes.c_int), _vp]),
+    "risa_gb_filter_destroy": (_i, [_vp]),
+    "risa_gb_filter_design_host": (_i, [_vp, _vp, ctypes.POINTER(ctypes.c_int), _vp]),
+    "risa_gb_backprojection_create": (_i, [_vp, _vp, _pp]),
+    "risa_gb_backprojection_enqueue": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "risa_gb_backprojection_enqueue_adjoint": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "risa_gb_backprojection_autotune": (_i, [_vp, _vp, _vp, _i, _vp, ctypes.POINTER(ctypes.c_int)]),
+    "risa_gb_backprojection_set_variant": (_i, [_vp, _i]),
+    "risa_gb_backprojection_variant_count": (_i, []),
+    "risa_gb_backprojection_destroy": (_i, [_vp]),
+    "risa_gb_masking_create": (_i, [_vp, _vp, _pp]),
+    "risa_gb_masking_workspace_bytes": (_sz, [_vp, _i]),
+    "risa_gb_masking_enqueue": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "risa_gb_masking_destroy": (_i, [_vp]),
+    "risa_gb_fbp_create": (_i, [_vp, _vp, _vp, _i, _vp, _i, _i, _pp]),
+    "risa_gb_fbp_enqueue": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
+    "risa_gb_fbp_graph_capture": (_i, [_vp, _vp, _vp, _i, _i, _vp, _pp]),
+    "risa_gb_graph_replay": (_i, [_vp, _vp]),
+    "risa_gb_graph_kernel_count": (_i, [_vp]),
+    "risa_gb_graph_destroy": (_i, [_vp]),
+    "risa_gb_fbp_run_host": (_i, [_vp, _vp, _vp, _i, _i]),
+    "risa_gb_fbp_intermediates": (_i, [_vp, _pp, _pp]),
+    "risa_gb_fbp_backprojection": (_vp, [_vp]),
+    "risa_gb_fbp_destroy": (_i, [_vp]),
+}
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load librisa_gb300.so (built by ``__graft_entry__.build()`` / ``risa_gb300.build``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m risa_gb300.build` "
+                              "(there is no CPU fallback)")
+        _lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(_lib, name)
+            fn.restype = res
+            fn.argtypes = args
+    return _lib
+
+
+def last_error() -> str:
+    return lib().risa_gb_last_error().decode()
+
+
+def _check(status: int, what: str):
+    if status != 0:
+        raise RisaError(status, what, last_error())
+
+
+def ptr(x) -> Optional[int]:
+    """Device/host address of an int, a torch tensor, a numpy array or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if hasattr(x, "ctypes"):
+        return x.ctypes.data
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def stream_ptr(stream) -> Optional[int]:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def make_geometry(n_planes=1, n_fan_det=432, n_fan_proj=500, n_par_proj=256, n_par_det=256,
+                  n_pixels=256, n_modules=27, source_offset=0.0, detector_diameter=480.0,
+                  image_width=200.0, image_center_x=0.0, image_center_y=0.0, rotation_offset=0.0,
+                  source_diameter: Sequence[float] = (430.0,), delta_x: Sequence[float] = (0.0,),
+                  delta_z: Sequence[float] = (1417.0,), source_angle: Sequence[float] = (360.0,)) -> Geometry:
+    g = Geometry()
+    lib().risa_gb_geometry_init(ctypes.byref(g))
+    g.n_planes, g.n_fan_det, g.n_fan_proj = n_planes, n_fan_det, n_fan_proj
+    g.n_par_proj, g.n_par_det, g.n_pixels, g.n_modules = n_par_proj, n_par_det, n_pixels, n_modules
+    g.source_offset, g.detector_diameter, g.image_width = source_offset, detector_diameter, image_width
+    g.image_center_x, g.image_center_y, g.rotation_offset = image_center_x, image_center_y, rotation_offset
+    for name, vals in (("source_diameter", source_diameter), ("delta_x", delta_x),
+                       ("delta_z", delta_z), ("source_angle", source_angle)):
+        arr = getattr(g, name)
+        vals = list(vals)
+        for k in range(MAX_PLANES):
+            arr[k] = float(vals[min(k, len(vals) - 1)])
+    return g
+
+
+def make_params(quirks=QUIRKS_NONE, filter_type="ramp", cutoff=1.0, pad=0, interp=INTERP_LINEAR,
+                defects=False, thresh_min=0.67, thresh_max=1.5, relevant_mask=False,
+                lower_lim_offset=0.0, upper_lim_offset=0.0, fix_points=(0, 0, 0, 0, 0, 0),
+                masking=False, masking_value=0.0, normalize=False, repair_reference=True) -> Params:
+    p = Params()
+    lib().risa_gb_params_init(ctypes.byref(p))
+    p.quirks = quirks
+    p.filter_type = FILTERS[filter_type] if isinstance(filter_type, str) else int(filter_type)
+    p.cutoff, p.pad, p.interp = cutoff, pad, interp
+    p.defects, p.thresh_min, p.thresh_max = int(defects), thresh_min, thresh_max
+    p.relevant_mask = int(relevant_mask)
+    p.lower_lim_offset, p.upper_lim_offset = lower_lim_offset, upper_lim_offset
+    p.xa, p.xb, p.xc, p.xd, p.xe, p.xf = (int(v) for v in fix_points)
+    p.masking, p.masking_value, p.normalize = int(masking), masking_value, int(normalize)
+    p.repair_reference = int(repair_reference)
+    return p
+
+
+def load_config(path: str):
+    g, p = Geometry(), Params()
+    _check(lib().risa_gb_config_load(path.encode(), ctypes.byref(g), ctypes.byref(p)), "config_load")
+    return g, p
+
+
+def geometry_dict(g: Geometry) -> dict:
+    out = {f: getattr(g, f) for f, _ in Geometry._fields_ if f != "struct_size"}
+    for k in ("source_diameter", "delta_x", "delta_z", "source_angle"):
+        out[k] = list(out[k])[: g.n_planes]
+    return out
+
+
+class _Handle:
+    _destroy = None
+
+    def __init__(self):
+        self._h = ctypes.c_void_p()
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def close(self):
+        if self._h and self._h.value and self._destroy:
+            getattr(lib(), self._destroy)(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Defects(_Handle):
+    """DetectorInterpolation stage: defect detection + in-place repair of u16 frames."""
+    _destroy = "risa_gb_defects_destroy"
+
+    def __init__(self, geom: Geometry, params: Params, max_batch: int):
+        super().__init__()
+        _check(lib().risa_gb_defects_create(ctypes.byref(geom), ctypes.byref(params), max_batch,
+                                            ctypes.byref(self._h)), "defects_create")
+
+    def workspace_bytes(self, batch: int) -> int:
+        return lib().risa_gb_defects_workspace_bytes(self._h, batch)
+
+    def enqueue(self, frames, batch: int, workspace, flags_out=None, stream=None):
+        _check(lib().risa_gb_defects_enqueue(self._h, ptr(frames), batch, ptr(flags_out), ptr(workspace),
+                                             stream_ptr(stream)), "defects_enqueue")
+
+
+class Attenuation(_Handle):
+    _destroy = "risa_gb_attenuation_destroy"
+
+    def __init__(self, geom: Geometry, params: Params, ref_frames, n_ref: int, dark_frames=None,
+                 n_dark: int = 0):
+        """ref_frames/dark_frames: host arrays [n][L][Pf][Df] uint16 (numpy)."""
+        super().__init__()
+        _check(lib().risa_gb_attenuation_create(ctypes.byref(geom), ctypes.byref(params), ptr(ref_frames),
+                                                n_ref, ptr(dark_frames), n_dark, ctypes.byref(self._h)),
+               "attenuation_create")
+        self.geom = geom
+
+    def enqueue(self, raw, out, plane: int, batch: int, stream=None):
+        _check(lib().risa_gb_attenuation_enqueue(self._h, ptr(raw), ptr(out), plane, batch,
+                                                 stream_ptr(stream)), "attenuation_enqueue")
+
+    def tables(self):
+        import numpy as np
+        g = self.geom
+        ref = np.zeros((g.n_planes, g.n_fan_proj, g.n_fan_det), np.float32)
+        dark = np.zeros((g.n_planes, g.n_fan_det), np.float32)
+        _check(lib().risa_gb_attenuation_tables(self._h, ptr(ref), ptr(dark)), "attenuation_tables")
+        return ref, dark
+
+
+class Fan2Para(_Handle):
+    _destroy = "risa_gb_fan2para_destroy"
+
+    def __init__(self, geom: Geometry, params: Params):
+        super().__init__()
+        _check(lib().risa_gb_fan2para_create(ctypes.byref(geom), ctypes.byref(params), ctypes.byref(self._h)),
+               "fan2para_create")
+
+    def enqueue(self, fan, par, plane: int, batch: int, stream=None):
+        _check(lib().risa_gb_fan2para_enqueue(self._h, ptr(fan), ptr(par), plane, batch, stream_ptr(stream)),
+               "fan2para_enqueue")
+
+    def enqueue_adjoint(self, par, fan, plane: int, batch: int, stream=None):
+        _check(lib().risa_gb_fan2para_enqueue_adjoint(self._h, ptr(par), ptr(fan), plane, batch,
+                                                      stream_ptr(stream)), "fan2para_enqueue_adjoint")
+
+
+def fan2para_tables_host(geom: Geometry, params: Params, plane: int = 0):
+    """Host-built gather table of one plane: (packed u32, u f32, v f32), each [4, Pp*Dp]."""
+    import numpy as np
+    n = 4 * geom.n_par_proj * geom.n_par_det
+    pk = np.zeros(n, np.uint32)
+    u = np.zeros(n, np.float32)
+    v = np.zeros(n, np.float32)
+    _check(lib().risa_gb_fan2para_tables_host(ctypes.byref(geom), ctypes.byref(params), plane, ptr(pk),
+                                              ptr(u), ptr(v)), "fan2para_tables_host")
+    return pk.reshape(4, -1), u.reshape(4, -1), v.reshape(4, -1)
+
+
+class Filter(_Handle):
+    _destroy = "risa_gb_filter_destroy"
+
+    def __init__(self, geom: Geometry, params: Params):
+        super().__init__()
+        _check(lib().risa_gb_filter_create(ctypes.byref(geom), ctypes.byref(params), ctypes.byref(self._h)),
+               "filter_create")
+
+    def enqueue(self, sino, batch: int, stream=None):
+        _check(lib().risa_gb_filter_enqueue(self._h, ptr(sino), batch, stream_ptr(stream)), "filter_enqueue")
+
+    def response(self):
+        import numpy as np
+        n = ctypes.c_int()
+        _check(lib().risa_gb_filter_response(self._h, ctypes.byref(n), None), "filter_response")
+        h = np.zeros(n.value // 2 + 1, np.float32)
+        _check(lib().risa_gb_filter_response(self._h, ctypes.byref(n), ptr(h)), "filter_response")
+        return n.value, h
+
+
+def filter_design_host(geom: Geometry, params: Params):
+    import numpy as np
+    n = ctypes.c_int()
+    _check(lib().risa_gb_filter_design_host(ctypes.byref(geom), ctypes.byref(params), ctypes.byref(n), None),
+           "filter_design_host")
+    h = np.zeros(n.value // 2 + 1, np.float32)
+    _check(lib().risa_gb_filter_design_host(ctypes.byref(geom), ctypes.byref(params), ctypes.byref(n), ptr(h)),
+           "filter_design_host")
+    return n.value, h
+
+
+class Backprojection(_Handle):
+    _destroy = "risa_gb_backprojection_destroy"
+
+    def __init__(self, geom: Geometry, params: Params, handle: Optional[int] = None):
+        super().__init__()
+        if handle is not None:  # borrowed from an FBP engine
+            self._h = ctypes.c_void_p(handle)
+            self._destroy = None
+            return
+        _check(lib().risa_gb_backprojection_create(ctypes.byref(geom), ctypes.byref(params),
+                                                   ctypes.byref(self._h)), "backprojection_create")
+
+    def enqueue(self, sino, img, batch: int, stream=None):
+        _check(lib().risa_gb_backprojection_enqueue(self._h, ptr(sino), ptr(img), batch, stream_ptr(stream)),
+               "backprojection_enqueue")
+
+    def enqueue_adjoint(self, img, sino, batch: int, stream=None):
+        _check(lib().risa_gb_backprojection_enqueue_adjoint(self._h, ptr(img), ptr(sino), batch,
+                                                            stream_ptr(stream)), "backprojection_adjoint")
+
+    def autotune(self, sino, img, batch: int, stream=None) -> int:
+        v = ctypes.c_int()
+        _check(lib().risa_gb_backprojection_autotune(self._h, ptr(sino), ptr(img), batch, stream_ptr(stream),
+                                                     ctypes.byref(v)), "backprojection_autotune")
+        return v.value
+
+    def set_variant(self, v: int):
+        _check(lib().risa_gb_backprojection_set_variant(self._h, v), "backprojection_set_variant")
+
+    @staticmethod
+    def variant_count() -> int:
+        return lib().risa_gb_backprojection_variant_count()
+
+
+class Masking(_Handle):
+    _destroy = "risa_gb_masking_destroy"
+
+    def __init__(self, geom: Geometry, params: Params):
+        super().__init__()
+        _check(lib().risa_gb_masking_create(ctypes.byref(geom), ctypes.byref(params), ctypes.byref(self._h)),
+               "masking_create")
+
+    def workspace_bytes(self, batch: int) -> int:
+        return lib().risa_gb_masking_workspace_bytes(self._h, batch)
+
+    def enqueue(self, img, batch: int, workspace=None, stream=None):
+        _check(lib().risa_gb_masking_enqueue(self._h, ptr(img), batch, ptr(workspace), stream_ptr(stream)),
+               "masking_enqueue")
+
+
+class Graph(_Handle):
+    """A captured whole-job CUDA graph (risa_gb_graph)."""
+    _destroy = "risa_gb_graph_destroy"
+    owner = None
+
+    def replay(self, stream=None):
+        _check(lib().risa_gb_graph_replay(self._h, stream_ptr(stream)), "graph_replay")
+
+    @property
+    def kernel_count(self) -> int:
+        return lib().risa_gb_graph_kernel_count(self._h)
+
+
+class FBP(_Handle):
+    """Whole chain, raw u16 fan frames -> images, batched, graph-capturable."""
+    _destroy = "risa_gb_fbp_destroy"
+
+    def __init__(self, geom: Geometry, params: Params, ref_frames, n_ref: int, dark_frames=None,
+                 n_dark: int = 0, max_batch: int = 1):
+        super().__init__()
+        _check(lib().risa_gb_fbp_create(ctypes.byref(geom), ctypes.byref(params), ptr(ref_frames), n_ref,
+                                        ptr(dark_frames), n_dark, max_batch, ctypes.byref(self._h)),
+               "fbp_create")
+        self.geom, self.params, self.max_batch = geom, params, max_batch
+
+    def enqueue(self, raw, img, plane: int, batch: int, stream=None):
+        _check(lib().risa_gb_fbp_enqueue(self._h, ptr(raw), ptr(img), plane, batch, stream_ptr(stream)),
+               "fbp_enqueue")
+
+    def graph_capture(self, raw, img, plane: int, n_frames: int, stream) -> "Graph":
+        """One CUDA graph reconstructing n_frames device frames (chunked by max_batch)."""
+        gr = Graph()
+        _check(lib().risa_gb_fbp_graph_capture(self._h, ptr(raw), ptr(img), plane, n_frames,
+                                               stream_ptr(stream), ctypes.byref(gr._h)), "fbp_graph_capture")
+        gr.owner = self
+        return gr
+
+    def run_host(self, host_raw, host_img, n_frames: int, plane: int):
+        _check(lib().risa_gb_fbp_run_host(self._h, ptr(host_raw), ptr(host_img), n_frames, plane),
+               "fbp_run_host")
+
+    def intermediates(self):
+        fan, par = ctypes.c_void_p(), ctypes.c_void_p()
+        _check(lib().risa_gb_fbp_intermediates(self._h, ctypes.byref(fan), ctypes.byref(par)),
+               "fbp_intermediates")
+        return fan.value, par.value
+
+    def backprojection(self) -> Backprojection:
+        return Backprojection(self.geom, self.params, handle=lib().risa_gb_fbp_backprojection(self._h))

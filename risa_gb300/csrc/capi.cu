@@ -1,0 +1,964 @@
+// C ABI: stage handles, the batched whole-chain engine with CUDA-graph
+// capture, and the host-buffer pipeline. Each stage handle replaces one of the
+// reference's stage classes (see include/risa_gb300.h for the mapping).
+#include "kernels.h"
+#include "risa_gb_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace risa_gb {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+risa_gb_status fail(risa_gb_status code, const std::string& msg) {
+   set_error(msg);
+   return code;
+}
+
+#define RG_CUDA(expr)                                                                         \
+   do {                                                                                       \
+      cudaError_t e_ = (expr);                                                                \
+      if (e_ != cudaSuccess)                                                                  \
+         return ::risa_gb::fail(RISA_GB_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+   } while (0)
+
+#define RG_TRY(expr)                        \
+   do {                                     \
+      risa_gb_status s_ = (expr);           \
+      if (s_ != RISA_GB_OK) return s_;      \
+   } while (0)
+
+namespace {
+// Device allocation owned by a handle.
+struct DevBuf {
+   void* p = nullptr;
+   size_t bytes = 0;
+   DevBuf() = default;
+   DevBuf(const DevBuf&) = delete;
+   DevBuf& operator=(const DevBuf&) = delete;
+   ~DevBuf() { release(); }
+   void release() {
+      if (p) cudaFree(p);
+      p = nullptr;
+      bytes = 0;
+   }
+   risa_gb_status alloc(size_t n) {
+      release();
+      if (n == 0) return RISA_GB_OK;
+      cudaError_t e = cudaMalloc(&p, n);
+      if (e != cudaSuccess) {
+         p = nullptr;
+         return fail(RISA_GB_ENOMEM, std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
+      }
+      bytes = n;
+      return RISA_GB_OK;
+   }
+   template <typename T>
+   risa_gb_status upload(const std::vector<T>& v) {
+      RG_TRY(alloc(sizeof(T) * v.size()));
+      if (!v.empty()) RG_CUDA(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+      return RISA_GB_OK;
+   }
+   template <typename T>
+   T* as() const { return static_cast<T*>(p); }
+};
+
+inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
+
+risa_gb_status check_plane(const Geometry& g, int plane) {
+   if (plane != RISA_GB_PLANES_INTERLEAVED && (plane < 0 || plane >= g.L))
+      return fail(RISA_GB_EINVAL, "plane out of range");
+   return RISA_GB_OK;
+}
+}  // namespace
+
+risa_gb_status import_geometry(const risa_gb_geometry* in, Geometry* g, bool need_fan, bool need_par,
+                               bool need_image) {
+   if (!in) return fail(RISA_GB_EINVAL, "geometry is NULL");
+   if (in->struct_size != sizeof(risa_gb_geometry))
+      return fail(RISA_GB_EINVAL, "geometry struct_size mismatch (initialise with risa_gb_geometry_init)");
+   g->L = in->n_planes;
+   g->Df = in->n_fan_det;
+   g->Pf = in->n_fan_proj;
+   g->Pp = in->n_par_proj;
+   g->Dp = in->n_par_det;
+   g->N = in->n_pixels;
+   g->modules = in->n_modules;
+   g->source_offset = in->source_offset;
+   g->detector_diameter = in->detector_diameter;
+   g->image_width = in->image_width;
+   g->image_center_x = in->image_center_x;
+   g->image_center_y = in->image_center_y;
+   g->rotation_offset = in->rotation_offset;
+   for (int k = 0; k < RISA_GB_MAX_PLANES; ++k) {
+      g->source_diameter[k] = in->source_diameter[k];
+      g->delta_x[k] = in->delta_x[k];
+      g->delta_z[k] = in->delta_z[k];
+      g->source_angle[k] = in->source_angle[k];
+   }
+   if (g->L < 1 || g->L > RISA_GB_MAX_PLANES) return fail(RISA_GB_EINVAL, "n_planes must be 1..4");
+   if (need_fan && (g->Df < 4 || g->Pf < 2 || g->Df > 16384 || g->Pf > 16384))
+      return fail(RISA_GB_EINVAL, "fan sinogram must be 2..16384 projections x 4..16384 detectors");
+   if (need_fan && g->Df > 8192)
+      return fail(RISA_GB_EUNSUPPORTED, "defect detection supports at most 8192 detectors");
+   if (need_par && (g->Pp < 1 || g->Dp < 2 || g->Pp > 65535 || g->Dp > 8192))
+      return fail(RISA_GB_EINVAL, "parallel sinogram must be 1..65535 angles x 2..8192 rays");
+   if (need_image && (g->N < 1 || g->N > 16384))
+      return fail(RISA_GB_EINVAL, "n_pixels must be 1..16384");
+   if (need_fan && need_par) {
+      if (g->detector_diameter <= 0 || g->image_width <= 0)
+         return fail(RISA_GB_EINVAL, "detector_diameter and image_width must be positive");
+      for (int k = 0; k < g->L; ++k)
+         if (g->source_diameter[k] <= 0) return fail(RISA_GB_EINVAL, "source_diameter must be positive");
+   }
+   return RISA_GB_OK;
+}
+
+risa_gb_status import_params(const risa_gb_params* in, Params* p) {
+   if (!in) return fail(RISA_GB_EINVAL, "params is NULL");
+   if (in->struct_size != sizeof(risa_gb_params))
+      return fail(RISA_GB_EINVAL, "params struct_size mismatch (initialise with risa_gb_params_init)");
+   p->quirks = in->quirks;
+   p->filter_type = in->filter_type;
+   p->cutoff = in->cutoff;
+   p->pad = in->pad;
+   p->interp = in->interp;
+   p->defects = in->defects;
+   p->thresh_min = in->thresh_min;
+   p->thresh_max = in->thresh_max;
+   p->relevant_mask = in->relevant_mask;
+   p->lower_lim_offset = in->lower_lim_offset;
+   p->upper_lim_offset = in->upper_lim_offset;
+   p->xa = in->xa; p->xb = in->xb; p->xc = in->xc; p->xd = in->xd; p->xe = in->xe; p->xf = in->xf;
+   p->masking = in->masking;
+   p->masking_value = in->masking_value;
+   p->normalize = in->normalize;
+   p->repair_reference = in->repair_reference;
+   if (p->quirks != RISA_GB_QUIRKS_NONE && p->quirks != RISA_GB_QUIRKS_RISA)
+      return fail(RISA_GB_EINVAL, "unknown quirks mode");
+   if (p->filter_type < 0 || p->filter_type > 4) return fail(RISA_GB_EINVAL, "unknown filter type");
+   if (!(p->cutoff > 0.0)) return fail(RISA_GB_EINVAL, "cutoff must be positive");
+   if (p->interp < 0 || p->interp > 2) return fail(RISA_GB_EINVAL, "unknown interpolation");
+   return RISA_GB_OK;
+}
+
+}  // namespace risa_gb
+
+using namespace risa_gb;
+
+// ============================================================================ handles
+struct risa_gb_defects {
+   Geometry g;
+   Params p;
+   DefectCfg cfg;
+   int max_batch = 0;
+};
+
+struct risa_gb_attenuation {
+   Geometry g;
+   Params p;
+   DevBuf logden, dark, avg, mask;
+   int wpr = 0;
+   AttenuationCfg cfg(int plane) const {
+      AttenuationCfg c;
+      c.P = g.Pf; c.D = g.Df; c.L = g.L; c.plane = plane;
+      c.logden = logden.as<float>();
+      c.dark = dark.as<float>();
+      c.mask = p.relevant_mask ? mask.as<uint32_t>() : nullptr;
+      c.wpr = wpr;
+      c.quirk = p.quirks;
+      return c;
+   }
+};
+
+struct risa_gb_fan2para {
+   Geometry g;
+   Params p;
+   DevBuf packed, u, v;
+   DevBuf adj_rowptr, adj_col, adj_w;
+   int adj_nnz_stride = 0;
+   bool adj_ready = false;
+   F2PCfg cfg(int plane) const {
+      F2PCfg c;
+      c.Pf = g.Pf; c.Df = g.Df; c.Pp = g.Pp; c.Dp = g.Dp; c.L = g.L; c.plane = plane;
+      c.packed = packed.as<uint32_t>();
+      c.u = u.as<float>();
+      c.v = v.as<float>();
+      return c;
+   }
+};
+
+struct risa_gb_filter {
+   Geometry g;
+   Params p;
+   int len = 0;
+   std::vector<float> h_host;
+   DevBuf h, tw;
+   FilterCfg cfg() const {
+      FilterCfg c;
+      c.rows = g.Pp; c.Dp = g.Dp; c.len = len;
+      c.twiddle = tw.as<float2>();
+      c.h = h.as<float>();
+      return c;
+   }
+};
+
+struct risa_gb_backprojection {
+   Geometry g;
+   Params p;
+   DevBuf a, b, ad, bd, t0;
+   float norm = 0.f;
+   int variant = 0;
+   BPCfg cfg(bool fused_mask) const {
+      BPCfg c;
+      c.Pp = g.Pp; c.Dp = g.Dp; c.N = g.N;
+      c.a = a.as<float>(); c.b = b.as<float>(); c.t0 = t0.as<double>();
+      c.ad = ad.as<double>(); c.bd = bd.as<double>();
+      c.norm = norm;
+      c.masking = fused_mask ? 1 : 0;
+      c.mask_value = (float)p.masking_value;
+      c.interp = p.interp;
+      c.scale = (float)((double)g.Dp / (double)g.N);
+      return c;
+   }
+};
+
+struct risa_gb_masking {
+   Geometry g;
+   Params p;
+};
+
+struct risa_gb_graph {
+   cudaGraphExec_t exec = nullptr;
+   int kernels = 0;
+   ~risa_gb_graph() {
+      if (exec) cudaGraphExecDestroy(exec);
+   }
+};
+
+struct risa_gb_fbp {
+   Geometry g;
+   Params p;
+   int max_batch = 0;
+   risa_gb_defects* defects = nullptr;
+   risa_gb_attenuation* atten = nullptr;
+   risa_gb_fan2para* f2p = nullptr;
+   risa_gb_filter* filt = nullptr;
+   risa_gb_backprojection* bp = nullptr;
+   risa_gb_masking* mask = nullptr;
+   DevBuf fan, par, dws, mm;
+   // host pipeline
+   DevBuf raw_slot[2], img_slot[2];
+   cudaStream_t s_comp = nullptr, s_h2d = nullptr, s_d2h = nullptr;
+   cudaEvent_t ev_h2d[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr},
+               ev_d2h[2] = {nullptr, nullptr};
+   cudaGraphExec_t slot_exec[2] = {nullptr, nullptr};
+   int slot_plane = 0x7fffffff;
+};
+
+// ============================================================================ C ABI
+extern "C" {
+
+risa_gb_status risa_gb_params_init(risa_gb_params* p) {
+   if (!p) return fail(RISA_GB_EINVAL, "params is NULL");
+   std::memset(p, 0, sizeof(*p));
+   p->struct_size = sizeof(*p);
+   p->quirks = RISA_GB_QUIRKS_NONE;
+   p->filter_type = RISA_GB_FILTER_RAMP;
+   p->cutoff = 1.0;
+   p->pad = 0;
+   p->interp = RISA_GB_INTERP_LINEAR;
+   p->thresh_min = 0.67;
+   p->thresh_max = 1.5;
+   p->masking_value = 0.0;
+   p->repair_reference = 1;
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_geometry_init(risa_gb_geometry* g) {
+   if (!g) return fail(RISA_GB_EINVAL, "geometry is NULL");
+   std::memset(g, 0, sizeof(*g));
+   g->struct_size = sizeof(*g);
+   g->n_planes = 1;
+   for (int k = 0; k < RISA_GB_MAX_PLANES; ++k) g->source_angle[k] = 360.0;
+   return RISA_GB_OK;
+}
+
+const char* risa_gb_last_error(void) { return g_last_error.c_str(); }
+const char* risa_gb_version(void) { return "risa_gb300 0.1 (sm_103a)"; }
+
+risa_gb_status risa_gb_config_load(const char* path, risa_gb_geometry* g, risa_gb_params* p) {
+   return load_config(path, g, p);
+}
+
+// ---------------------------------------------------------------------------- defects
+risa_gb_status risa_gb_defects_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                      int max_batch, risa_gb_defects** out) {
+   if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_defects> h(new (std::nothrow) risa_gb_defects());
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, true, false, false));
+   RG_TRY(import_params(pi, &h->p));
+   if (max_batch < 1) return fail(RISA_GB_EINVAL, "max_batch must be >= 1");
+   h->max_batch = max_batch;
+   h->cfg.P = h->g.Pf;
+   h->cfg.D = h->g.Df;
+   h->cfg.thresh_min = h->p.thresh_min;
+   h->cfg.thresh_max = h->p.thresh_max;
+   h->cfg.quirk = h->p.quirks;
+   h->cfg.max_runs = h->g.Df / 2 + 2;
+   RG_CUDA(upload_defect_filter(0));
+   RG_CUDA(cudaStreamSynchronize(0));
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+size_t risa_gb_defects_workspace_bytes(const risa_gb_defects* h, int batch) {
+   if (!h || batch < 1) return 0;
+   return defects_workspace_bytes(h->cfg.D, batch, h->cfg.max_runs);
+}
+
+risa_gb_status risa_gb_defects_enqueue(risa_gb_defects* h, uint16_t* frames, int batch,
+                                       int32_t* flags_out, void* workspace, void* stream) {
+   if (!h || !frames || !workspace) return fail(RISA_GB_EINVAL, "null handle, frames or workspace");
+   if (batch < 0 || batch > h->max_batch) return fail(RISA_GB_EINVAL, "batch exceeds max_batch");
+   DefectWorkspace ws = defects_carve(workspace, h->cfg.D, batch, h->cfg.max_runs);
+   RG_CUDA(launch_defect_detect(frames, batch, h->cfg, ws, flags_out, S(stream)));
+   RG_CUDA(launch_defect_repair(frames, batch, h->cfg, ws, S(stream)));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_defects_destroy(risa_gb_defects* h) {
+   delete h;
+   return RISA_GB_OK;
+}
+
+// ---------------------------------------------------------------------------- attenuation
+risa_gb_status risa_gb_attenuation_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                          const uint16_t* ref_frames, int n_ref,
+                                          const uint16_t* dark_frames, int n_dark,
+                                          risa_gb_attenuation** out) {
+   if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_attenuation> h(new (std::nothrow) risa_gb_attenuation());
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, true, false, false));
+   RG_TRY(import_params(pi, &h->p));
+   if (!ref_frames || n_ref < 1) return fail(RISA_GB_EINVAL, "at least one reference frame is required");
+   const Geometry& g = h->g;
+   const size_t fs = (size_t)g.Pf * g.Df;
+   const size_t nref_frames = (size_t)n_ref * g.L;
+   DevBuf d_ref;
+   RG_TRY(d_ref.alloc(sizeof(uint16_t) * fs * nref_frames));
+   RG_CUDA(cudaMemcpy(d_ref.p, ref_frames, sizeof(uint16_t) * fs * nref_frames, cudaMemcpyHostToDevice));
+   if (h->p.repair_reference) {
+      // Attenuation::init repairs every reference frame before averaging (Attenuation.cu:191-196)
+      risa_gb_defects* dh = nullptr;
+      RG_TRY(risa_gb_defects_create(gi, pi, (int)nref_frames, &dh));
+      std::unique_ptr<risa_gb_defects, risa_gb_status (*)(risa_gb_defects*)> guard(dh, risa_gb_defects_destroy);
+      DevBuf ws;
+      RG_TRY(ws.alloc(risa_gb_defects_workspace_bytes(dh, (int)nref_frames)));
+      RG_TRY(risa_gb_defects_enqueue(dh, d_ref.as<uint16_t>(), (int)nref_frames, nullptr, ws.p, nullptr));
+      RG_CUDA(cudaDeviceSynchronize());
+   }
+   RG_TRY(h->avg.alloc(sizeof(float) * fs * g.L));
+   RG_TRY(h->dark.alloc(sizeof(float) * g.Df * g.L));
+   RG_TRY(h->logden.alloc(sizeof(float) * fs * g.L));
+   RG_CUDA(launch_reference_average(d_ref.as<uint16_t>(), n_ref, g.L, g.Pf, g.Df, h->p.quirks,
+                                    h->avg.as<float>(), 0));
+   if (dark_frames && n_dark > 0) {
+      const size_t nd = (size_t)n_dark * g.L;
+      DevBuf d_dark;
+      RG_TRY(d_dark.alloc(sizeof(uint16_t) * fs * nd));
+      RG_CUDA(cudaMemcpy(d_dark.p, dark_frames, sizeof(uint16_t) * fs * nd, cudaMemcpyHostToDevice));
+      RG_CUDA(launch_dark_average(d_dark.as<uint16_t>(), n_dark, g.L, g.Pf, g.Df, h->p.quirks,
+                                  h->dark.as<float>(), 0));
+      RG_CUDA(cudaDeviceSynchronize());
+   } else {
+      RG_CUDA(cudaMemset(h->dark.p, 0, h->dark.bytes));
+   }
+   if (h->p.quirks != RISA_GB_QUIRKS_RISA) {
+      // dark repair of Attenuation.cu:207-216 (a no-op in RISA mode, where the
+      // dark average is zero), with a circular neighbour wrap
+      std::vector<float> dk((size_t)g.Df * g.L);
+      RG_CUDA(cudaMemcpy(dk.data(), h->dark.p, h->dark.bytes, cudaMemcpyDeviceToHost));
+      bool changed = false;
+      for (int k = 0; k < g.L; ++k)
+         for (int d = 0; d < g.Df; ++d) {
+            float* row = dk.data() + (size_t)k * g.Df;
+            if (row[d] > 300.0f) {
+               row[d] = (float)(0.5 * ((double)row[(d + 1) % g.Df] + (double)row[(d + g.Df - 1) % g.Df]));
+               changed = true;
+            }
+         }
+      if (changed) RG_CUDA(cudaMemcpy(h->dark.p, dk.data(), h->dark.bytes, cudaMemcpyHostToDevice));
+   }
+   RG_CUDA(launch_logden(h->avg.as<float>(), h->dark.as<float>(), g.L, g.Pf, g.Df, h->logden.as<float>(), 0));
+   if (h->p.relevant_mask) {
+      std::vector<uint32_t> bits;
+      build_relevant_mask_bits(g, h->p, &bits, &h->wpr);
+      RG_TRY(h->mask.upload(bits));
+   }
+   RG_CUDA(cudaDeviceSynchronize());
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_attenuation_enqueue(risa_gb_attenuation* h, const uint16_t* raw, float* out,
+                                           int plane, int batch, void* stream) {
+   if (!h || !raw || !out) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (batch < 0) return fail(RISA_GB_EINVAL, "negative batch");
+   RG_TRY(check_plane(h->g, plane));
+   RG_CUDA(launch_attenuation(raw, out, batch, h->cfg(plane), nullptr, 0, S(stream)));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_attenuation_tables(const risa_gb_attenuation* h, float* host_ref, float* host_dark) {
+   if (!h) return fail(RISA_GB_EINVAL, "null handle");
+   if (host_ref) RG_CUDA(cudaMemcpy(host_ref, h->avg.p, h->avg.bytes, cudaMemcpyDeviceToHost));
+   if (host_dark) RG_CUDA(cudaMemcpy(host_dark, h->dark.p, h->dark.bytes, cudaMemcpyDeviceToHost));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_attenuation_destroy(risa_gb_attenuation* h) {
+   delete h;
+   return RISA_GB_OK;
+}
+
+// ---------------------------------------------------------------------------- fan2para
+risa_gb_status risa_gb_fan2para_tables_host(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                            int plane, uint32_t* packed, float* u, float* v) {
+   Geometry g;
+   Params p;
+   RG_TRY(import_geometry(gi, &g, true, true, false));
+   RG_TRY(import_params(pi, &p));
+   if (!packed || !u || !v) return fail(RISA_GB_EINVAL, "null output");
+   F2PGather t;
+   RG_TRY(build_f2p_gather(g, p, plane, &t));
+   std::memcpy(packed, t.packed.data(), sizeof(uint32_t) * t.packed.size());
+   std::memcpy(u, t.u.data(), sizeof(float) * t.u.size());
+   std::memcpy(v, t.v.data(), sizeof(float) * t.v.size());
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fan2para_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                       risa_gb_fan2para** out) {
+   if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_fan2para> h(new (std::nothrow) risa_gb_fan2para());
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, true, true, false));
+   RG_TRY(import_params(pi, &h->p));
+   std::vector<F2PGather> planes;
+   RG_TRY(build_f2p_gather_all(h->g, h->p, &planes));
+   std::vector<uint32_t> pk;
+   std::vector<float> u, v;
+   for (auto& t : planes) {
+      pk.insert(pk.end(), t.packed.begin(), t.packed.end());
+      u.insert(u.end(), t.u.begin(), t.u.end());
+      v.insert(v.end(), t.v.begin(), t.v.end());
+   }
+   RG_TRY(h->packed.upload(pk));
+   RG_TRY(h->u.upload(u));
+   RG_TRY(h->v.upload(v));
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fan2para_enqueue(risa_gb_fan2para* h, const float* fan, float* par, int plane,
+                                        int batch, void* stream) {
+   if (!h || !fan || !par) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (batch < 0) return fail(RISA_GB_EINVAL, "negative batch");
+   RG_TRY(check_plane(h->g, plane));
+   RG_CUDA(launch_fan2para(fan, par, batch, h->cfg(plane), S(stream)));
+   return RISA_GB_OK;
+}
+
+// Transposed rebinning table (CSR over fan samples), built on the host from
+// the gather table: par[o] = sum_s c_s * sum_corners w * fan[t] becomes
+// fan[t] = sum over (o, corner) of c_s * w * par[o].
+static risa_gb_status build_adjoint(risa_gb_fan2para* h) {
+   const Geometry& g = h->g;
+   const int no = g.Pp * g.Dp, nf = g.Pf * g.Df;
+   std::vector<F2PGather> planes;
+   RG_TRY(build_f2p_gather_all(g, h->p, &planes));
+   std::vector<int> rowptr_all;
+   std::vector<int> col_all;
+   std::vector<float> w_all;
+   size_t stride = 0;
+   std::vector<std::vector<std::pair<int, float>>> per_fan;
+   std::vector<std::vector<int>> cols(g.L);
+   std::vector<std::vector<float>> ws(g.L);
+   std::vector<std::vector<int>> rps(g.L);
+   for (int k = 0; k < g.L; ++k) {
+      const F2PGather& t = planes[k];
+      std::vector<int> counts(nf + 1, 0);
+      std::vector<std::pair<int, std::pair<int, float>>> entries;
+      entries.reserve((size_t)no * 8);
+      for (int o = 0; o < no; ++o) {
+         int na = 0, nb = 0;
+         for (int s = 0; s < 4; ++s)
+            if (t.packed[(size_t)s * no + o] >> 31) (s < 2 ? na : nb)++;
+         for (int s = 0; s < 4; ++s) {
+            const uint32_t pk = t.packed[(size_t)s * no + o];
+            if (!(pk >> 31)) continue;
+            const int n = s < 2 ? na : nb;
+            const float c = 0.5f * (n == 2 ? 0.5f : 1.0f);
+            const int tb = (int)((pk >> 16) & 0x7FFF), gb = (int)(pk & 0xFFFF);
+            const int ta = (tb + 1) % g.Pf, ga = (gb + 1) % g.Df;
+            const float u = t.u[(size_t)s * no + o], v = t.v[(size_t)s * no + o];
+            const int idx[4] = {tb * g.Df + gb, tb * g.Df + ga, ta * g.Df + gb, ta * g.Df + ga};
+            const float wt[4] = {(1 - u) * (1 - v), (1 - u) * v, u * (1 - v), u * v};
+            for (int q = 0; q < 4; ++q) entries.push_back({idx[q], {o, c * wt[q]}});
+         }
+      }
+      std::stable_sort(entries.begin(), entries.end(),
+                       [](const auto& a, const auto& b) { return a.first < b.first; });
+      rps[k].assign(nf + 1, 0);
+      for (auto& e : entries) rps[k][e.first + 1]++;
+      for (int i = 0; i < nf; ++i) rps[k][i + 1] += rps[k][i];
+      cols[k].resize(entries.size());
+      ws[k].resize(entries.size());
+      for (size_t i = 0; i < entries.size(); ++i) {
+         cols[k][i] = entries[i].second.first;
+         ws[k][i] = entries[i].second.second;
+      }
+      stride = std::max(stride, entries.size());
+   }
+   for (int k = 0; k < g.L; ++k) {
+      rowptr_all.insert(rowptr_all.end(), rps[k].begin(), rps[k].end());
+      cols[k].resize(stride, 0);
+      ws[k].resize(stride, 0.f);
+      col_all.insert(col_all.end(), cols[k].begin(), cols[k].end());
+      w_all.insert(w_all.end(), ws[k].begin(), ws[k].end());
+   }
+   RG_TRY(h->adj_rowptr.upload(rowptr_all));
+   RG_TRY(h->adj_col.upload(col_all));
+   RG_TRY(h->adj_w.upload(w_all));
+   h->adj_nnz_stride = (int)stride;
+   h->adj_ready = true;
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fan2para_enqueue_adjoint(risa_gb_fan2para* h, const float* par, float* fan,
+                                                int plane, int batch, void* stream) {
+   if (!h || !par || !fan) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   RG_TRY(check_plane(h->g, plane));
+   if (!h->adj_ready) {
+      // one-time table build (allocates); later calls are allocation-free
+      RG_CUDA(cudaStreamSynchronize(S(stream)));
+      RG_TRY(build_adjoint(h));
+   }
+   F2PAdjCfg c;
+   c.Pf = h->g.Pf; c.Df = h->g.Df; c.Pp = h->g.Pp; c.Dp = h->g.Dp; c.L = h->g.L; c.plane = plane;
+   c.row_ptr = h->adj_rowptr.as<int>();
+   c.col = h->adj_col.as<int>();
+   c.w = h->adj_w.as<float>();
+   c.nnz_stride = h->adj_nnz_stride;
+   RG_CUDA(launch_fan2para_adjoint(par, fan, batch, c, S(stream)));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fan2para_destroy(risa_gb_fan2para* h) {
+   delete h;
+   return RISA_GB_OK;
+}
+
+// ---------------------------------------------------------------------------- filter
+risa_gb_status risa_gb_filter_design_host(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                          int* len, float* hout) {
+   Geometry g;
+   Params p;
+   RG_TRY(import_geometry(gi, &g, false, true, false));
+   RG_TRY(import_params(pi, &p));
+   std::vector<float> h;
+   int l = 0;
+   RG_TRY(design_filter(g, p, &l, &h));
+   if (len) *len = l;
+   if (hout) std::memcpy(hout, h.data(), sizeof(float) * h.size());
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_filter_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                     risa_gb_filter** out) {
+   if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_filter> h(new (std::nothrow) risa_gb_filter());
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, false, true, false));
+   RG_TRY(import_params(pi, &h->p));
+   RG_TRY(design_filter(h->g, h->p, &h->len, &h->h_host));
+   std::vector<float> tw(h->len);  // interleaved (re, im) of exp(-2 pi i k / len), k < len/2
+   for (int k = 0; k < h->len / 2; ++k) {
+      const double ang = -2.0 * 3.14159265358979323846 * (double)k / (double)h->len;
+      tw[2 * k] = (float)std::cos(ang);
+      tw[2 * k + 1] = (float)std::sin(ang);
+   }
+   RG_TRY(h->tw.upload(tw));
+   RG_TRY(h->h.upload(h->h_host));
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_filter_enqueue(risa_gb_filter* h, float* sino, int batch, void* stream) {
+   if (!h || !sino) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (batch < 0) return fail(RISA_GB_EINVAL, "negative batch");
+   RG_CUDA(launch_filter(sino, batch, h->cfg(), S(stream)));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_filter_response(const risa_gb_filter* h, int* len, float* host_h) {
+   if (!h) return fail(RISA_GB_EINVAL, "null handle");
+   if (len) *len = h->len;
+   if (host_h) std::memcpy(host_h, h->h_host.data(), sizeof(float) * h->h_host.size());
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_filter_destroy(risa_gb_filter* h) {
+   delete h;
+   return RISA_GB_OK;
+}
+
+// ---------------------------------------------------------------------------- backprojection
+risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                             risa_gb_backprojection** out) {
+   if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_backprojection> h(new (std::nothrow) risa_gb_backprojection());
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, false, true, true));
+   RG_TRY(import_params(pi, &h->p));
+   BPTables t;
+   build_bp_tables(h->g, h->p, &t);
+   RG_TRY(h->a.upload(t.a));
+   RG_TRY(h->b.upload(t.b));
+   RG_TRY(h->t0.upload(t.t0));
+   RG_TRY(h->ad.upload(t.ad));
+   RG_TRY(h->bd.upload(t.bd));
+   h->norm = t.norm;
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+static risa_gb_status bp_run(risa_gb_backprojection* h, const float* sino, float* img, int batch,
+                             bool fused_mask, void* stream) {
+   RG_CUDA(launch_backprojection(sino, img, batch, h->cfg(fused_mask), h->variant, S(stream)));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_backprojection_enqueue(risa_gb_backprojection* h, const float* sino, float* img,
+                                              int batch, void* stream) {
+   if (!h || !sino || !img) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (batch < 0) return fail(RISA_GB_EINVAL, "negative batch");
+   const bool fused = h->p.masking && !h->p.normalize;
+   return bp_run(h, sino, img, batch, fused, stream);
+}
+
+risa_gb_status risa_gb_backprojection_enqueue_adjoint(risa_gb_backprojection* h, const float* img,
+                                                      float* sino, int batch, void* stream) {
+   if (!h || !sino || !img) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (h->p.interp != RISA_GB_INTERP_LINEAR)
+      return fail(RISA_GB_EUNSUPPORTED, "the adjoint is defined for linear interpolation");
+   RG_CUDA(launch_backprojection_adjoint(img, sino, batch, h->cfg(false), S(stream)));
+   return RISA_GB_OK;
+}
+
+int risa_gb_backprojection_variant_count(void) { return bp_variant_count(); }
+
+risa_gb_status risa_gb_backprojection_set_variant(risa_gb_backprojection* h, int variant) {
+   if (!h || variant < 0 || variant >= bp_variant_count()) return fail(RISA_GB_EINVAL, "bad variant");
+   h->variant = variant;
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_backprojection_autotune(risa_gb_backprojection* h, const float* sino, float* img,
+                                               int batch, void* stream, int* variant_out) {
+   if (!h || !sino || !img || batch < 1) return fail(RISA_GB_EINVAL, "bad autotune arguments");
+   cudaStream_t st = S(stream);
+   cudaEvent_t e0, e1;
+   RG_CUDA(cudaEventCreate(&e0));
+   RG_CUDA(cudaEventCreate(&e1));
+   const bool fused = h->p.masking && !h->p.normalize;
+   float best = 1e30f;
+   int best_v = 0;
+   for (int v = 0; v < bp_variant_count(); ++v) {
+      h->variant = v;
+      RG_TRY(bp_run(h, sino, img, batch, fused, stream));  // warm-up
+      RG_CUDA(cudaEventRecord(e0, st));
+      for (int r = 0; r < 3; ++r) RG_TRY(bp_run(h, sino, img, batch, fused, stream));
+      RG_CUDA(cudaEventRecord(e1, st));
+      RG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      RG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) { best = ms; best_v = v; }
+   }
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   h->variant = best_v;
+   if (variant_out) *variant_out = best_v;
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_backprojection_destroy(risa_gb_backprojection* h) {
+   delete h;
+   return RISA_GB_OK;
+}
+
+// ---------------------------------------------------------------------------- masking
+risa_gb_status risa_gb_masking_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                      risa_gb_masking** out) {
+   if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_masking> h(new (std::nothrow) risa_gb_masking());
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, false, false, true));
+   RG_TRY(import_params(pi, &h->p));
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+size_t risa_gb_masking_workspace_bytes(const risa_gb_masking* h, int batch) {
+   if (!h || batch < 1) return 0;
+   return sizeof(unsigned int) * 2 * (size_t)batch;
+}
+
+risa_gb_status risa_gb_masking_enqueue(risa_gb_masking* h, float* img, int batch, void* workspace,
+                                       void* stream) {
+   if (!h || !img) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (h->p.normalize && !workspace) return fail(RISA_GB_EINVAL, "normalisation needs a workspace");
+   RG_CUDA(launch_mask(img, batch, h->g.N, (float)h->p.masking_value, h->p.normalize,
+                       static_cast<float*>(workspace), 1, S(stream)));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_masking_destroy(risa_gb_masking* h) {
+   delete h;
+   return RISA_GB_OK;
+}
+
+// ---------------------------------------------------------------------------- whole chain
+risa_gb_status risa_gb_fbp_destroy(risa_gb_fbp* h) {
+   if (!h) return RISA_GB_OK;
+   for (int i = 0; i < 2; ++i) {
+      if (h->slot_exec[i]) cudaGraphExecDestroy(h->slot_exec[i]);
+      if (h->ev_h2d[i]) cudaEventDestroy(h->ev_h2d[i]);
+      if (h->ev_comp[i]) cudaEventDestroy(h->ev_comp[i]);
+      if (h->ev_d2h[i]) cudaEventDestroy(h->ev_d2h[i]);
+   }
+   if (h->s_comp) cudaStreamDestroy(h->s_comp);
+   if (h->s_h2d) cudaStreamDestroy(h->s_h2d);
+   if (h->s_d2h) cudaStreamDestroy(h->s_d2h);
+   risa_gb_defects_destroy(h->defects);
+   risa_gb_attenuation_destroy(h->atten);
+   risa_gb_fan2para_destroy(h->f2p);
+   risa_gb_filter_destroy(h->filt);
+   risa_gb_backprojection_destroy(h->bp);
+   risa_gb_masking_destroy(h->mask);
+   delete h;
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fbp_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                  const uint16_t* ref_frames, int n_ref, const uint16_t* dark_frames,
+                                  int n_dark, int max_batch, risa_gb_fbp** out) {
+   if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_fbp, risa_gb_status (*)(risa_gb_fbp*)> h(new (std::nothrow) risa_gb_fbp(),
+                                                                    risa_gb_fbp_destroy);
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, true, true, true));
+   RG_TRY(import_params(pi, &h->p));
+   if (max_batch < 1) return fail(RISA_GB_EINVAL, "max_batch must be >= 1");
+   h->max_batch = max_batch;
+   const Geometry& g = h->g;
+   if (h->p.defects) RG_TRY(risa_gb_defects_create(gi, pi, max_batch, &h->defects));
+   RG_TRY(risa_gb_attenuation_create(gi, pi, ref_frames, n_ref, dark_frames, n_dark, &h->atten));
+   RG_TRY(risa_gb_fan2para_create(gi, pi, &h->f2p));
+   RG_TRY(risa_gb_filter_create(gi, pi, &h->filt));
+   RG_TRY(risa_gb_backprojection_create(gi, pi, &h->bp));
+   RG_TRY(risa_gb_masking_create(gi, pi, &h->mask));
+   RG_TRY(h->fan.alloc(sizeof(float) * (size_t)max_batch * g.Pf * g.Df));
+   RG_TRY(h->par.alloc(sizeof(float) * (size_t)max_batch * g.Pp * g.Dp));
+   if (h->defects) RG_TRY(h->dws.alloc(risa_gb_defects_workspace_bytes(h->defects, max_batch)));
+   RG_TRY(h->mm.alloc(sizeof(unsigned int) * 2 * (size_t)max_batch));
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane, int batch,
+                                   void* stream) {
+   if (!h || !raw || !img) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (batch < 0 || batch > h->max_batch) return fail(RISA_GB_EINVAL, "batch exceeds max_batch");
+   RG_TRY(check_plane(h->g, plane));
+   cudaStream_t st = S(stream);
+   float* fan = h->fan.as<float>();
+   float* par = h->par.as<float>();
+   if (h->defects) {
+      const DefectCfg& dc = h->defects->cfg;
+      DefectWorkspace ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs);
+      RG_CUDA(launch_defect_detect(raw, batch, dc, ws, nullptr, st));
+      RG_CUDA(launch_attenuation(raw, fan, batch, h->atten->cfg(plane), &ws, dc.max_runs, st));
+   } else {
+      RG_CUDA(launch_attenuation(raw, fan, batch, h->atten->cfg(plane), nullptr, 0, st));
+   }
+   RG_CUDA(launch_fan2para(fan, par, batch, h->f2p->cfg(plane), st));
+   RG_CUDA(launch_filter(par, batch, h->filt->cfg(), st));
+   const bool fused = h->p.masking && !h->p.normalize;
+   RG_TRY(bp_run(h->bp, par, img, batch, fused, stream));
+   if (h->p.normalize)
+      RG_CUDA(launch_mask(img, batch, h->g.N, (float)h->p.masking_value, 1, h->mm.as<float>(),
+                          h->p.masking, st));
+   return RISA_GB_OK;
+}
+
+// Captures the chunked reconstruction of n_frames frames on stream `st`.
+static risa_gb_status capture(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane, int n_frames,
+                              cudaStream_t st, cudaGraphExec_t* exec_out, int* kernels) {
+   const Geometry& g = h->g;
+   const size_t fs = (size_t)g.Pf * g.Df, is = (size_t)g.N * g.N;
+   const int B = h->max_batch;
+   if (plane == RISA_GB_PLANES_INTERLEAVED && n_frames > B && B % g.L != 0)
+      return fail(RISA_GB_EINVAL, "interleaved planes need max_batch to be a multiple of n_planes");
+   cudaGraph_t graph = nullptr;
+   RG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+   risa_gb_status s = RISA_GB_OK;
+   for (int first = 0; first < n_frames && s == RISA_GB_OK; first += B) {
+      const int nb = std::min(B, n_frames - first);
+      s = risa_gb_fbp_enqueue(h, raw + (size_t)first * fs, img + (size_t)first * is, plane, nb, st);
+   }
+   cudaError_t e = cudaStreamEndCapture(st, &graph);
+   if (s != RISA_GB_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return s;
+   }
+   if (e != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+   if (kernels) {
+      size_t n = 0;
+      cudaGraphGetNodes(graph, nullptr, &n);
+      std::vector<cudaGraphNode_t> nodes(n);
+      if (n) cudaGraphGetNodes(graph, nodes.data(), &n);
+      int k = 0;
+      for (auto nd : nodes) {
+         cudaGraphNodeType t;
+         if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+      }
+      *kernels = k;
+   }
+   cudaGraphExec_t exec = nullptr;
+   e = cudaGraphInstantiate(&exec, graph, 0);
+   cudaGraphDestroy(graph);
+   if (e != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+   *exec_out = exec;
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fbp_graph_capture(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane,
+                                         int n_frames, void* stream, risa_gb_graph** out) {
+   if (!h || !raw || !img || !out) return fail(RISA_GB_EINVAL, "null handle, buffer or output");
+   if (!stream) return fail(RISA_GB_EINVAL, "graph capture needs a non-default stream");
+   if (n_frames < 1) return fail(RISA_GB_EINVAL, "n_frames must be >= 1");
+   RG_TRY(check_plane(h->g, plane));
+   *out = nullptr;
+   std::unique_ptr<risa_gb_graph> gr(new (std::nothrow) risa_gb_graph());
+   if (!gr) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(capture(h, raw, img, plane, n_frames, S(stream), &gr->exec, &gr->kernels));
+   *out = gr.release();
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_graph_replay(risa_gb_graph* g, void* stream) {
+   if (!g || !g->exec) return fail(RISA_GB_EINVAL, "no captured graph");
+   RG_CUDA(cudaGraphLaunch(g->exec, S(stream)));
+   return RISA_GB_OK;
+}
+
+int risa_gb_graph_kernel_count(const risa_gb_graph* g) { return g ? g->kernels : 0; }
+
+risa_gb_status risa_gb_graph_destroy(risa_gb_graph* g) {
+   delete g;
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, float* host_img,
+                                    int n_frames, int plane) {
+   if (!h || !host_raw || !host_img || n_frames < 0) return fail(RISA_GB_EINVAL, "bad arguments");
+   RG_TRY(check_plane(h->g, plane));
+   const Geometry& g = h->g;
+   const size_t fs = (size_t)g.Pf * g.Df, is = (size_t)g.N * g.N;
+   const int B = h->max_batch;
+   if (plane == RISA_GB_PLANES_INTERLEAVED && B % g.L != 0)
+      return fail(RISA_GB_EINVAL, "interleaved planes need max_batch to be a multiple of n_planes");
+   if (!h->s_comp) {
+      RG_CUDA(cudaStreamCreateWithFlags(&h->s_comp, cudaStreamNonBlocking));
+      RG_CUDA(cudaStreamCreateWithFlags(&h->s_h2d, cudaStreamNonBlocking));
+      RG_CUDA(cudaStreamCreateWithFlags(&h->s_d2h, cudaStreamNonBlocking));
+      for (int i = 0; i < 2; ++i) {
+         RG_CUDA(cudaEventCreateWithFlags(&h->ev_h2d[i], cudaEventDisableTiming));
+         RG_CUDA(cudaEventCreateWithFlags(&h->ev_comp[i], cudaEventDisableTiming));
+         RG_CUDA(cudaEventCreateWithFlags(&h->ev_d2h[i], cudaEventDisableTiming));
+         RG_TRY(h->raw_slot[i].alloc(sizeof(uint16_t) * fs * B));
+         RG_TRY(h->img_slot[i].alloc(sizeof(float) * is * B));
+      }
+   }
+   if (h->slot_plane != plane) {
+      for (int i = 0; i < 2; ++i) {
+         if (h->slot_exec[i]) cudaGraphExecDestroy(h->slot_exec[i]);
+         h->slot_exec[i] = nullptr;
+         RG_TRY(capture(h, h->raw_slot[i].as<uint16_t>(), h->img_slot[i].as<float>(), plane, B,
+                        h->s_comp, &h->slot_exec[i], nullptr));
+      }
+      h->slot_plane = plane;
+   }
+   const int chunks = (n_frames + B - 1) / B;
+   for (int c = 0; c < chunks; ++c) {
+      const int slot = c & 1;
+      const int first = c * B;
+      const int nb = std::min(B, n_frames - first);
+      // slot buffers are reused every second chunk: wait for their last readers
+      RG_CUDA(cudaStreamWaitEvent(h->s_h2d, h->ev_comp[slot], 0));
+      RG_CUDA(cudaMemcpyAsync(h->raw_slot[slot].p, host_raw + (size_t)first * fs,
+                              sizeof(uint16_t) * fs * nb, cudaMemcpyHostToDevice, h->s_h2d));
+      RG_CUDA(cudaEventRecord(h->ev_h2d[slot], h->s_h2d));
+      RG_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_h2d[slot], 0));
+      RG_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_d2h[slot], 0));
+      // a chunk starting at a multiple of B keeps the interleaved plane phase
+      if (nb == B) {
+         RG_CUDA(cudaGraphLaunch(h->slot_exec[slot], h->s_comp));
+      } else {
+         RG_TRY(risa_gb_fbp_enqueue(h, h->raw_slot[slot].as<uint16_t>(), h->img_slot[slot].as<float>(),
+                                    plane, nb, h->s_comp));
+      }
+      RG_CUDA(cudaEventRecord(h->ev_comp[slot], h->s_comp));
+      RG_CUDA(cudaStreamWaitEvent(h->s_d2h, h->ev_comp[slot], 0));
+      RG_CUDA(cudaMemcpyAsync(host_img + (size_t)first * is, h->img_slot[slot].p, sizeof(float) * is * nb,
+                              cudaMemcpyDeviceToHost, h->s_d2h));
+      RG_CUDA(cudaEventRecord(h->ev_d2h[slot], h->s_d2h));
+   }
+   RG_CUDA(cudaStreamSynchronize(h->s_d2h));
+   RG_CUDA(cudaStreamSynchronize(h->s_comp));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fbp_intermediates(risa_gb_fbp* h, float** fan, float** par) {
+   if (!h) return fail(RISA_GB_EINVAL, "null handle");
+   if (fan) *fan = h->fan.as<float>();
+   if (par) *par = h->par.as<float>();
+   return RISA_GB_OK;
+}
+
+risa_gb_backprojection* risa_gb_fbp_backprojection(risa_gb_fbp* h) { return h ? h->bp : nullptr; }
+
+}  // extern "C"

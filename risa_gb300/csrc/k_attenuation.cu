@@ -1,0 +1,240 @@
+// Attenuation: uint16 raw fan frames -> FP32 line integrals.
+//
+// Reference: computeAttenuation (Attenuation.cu:416-444) computes, per sample,
+// -log(max(raw - dark, 1e-5) / max(ref - dark, 1e-5)) * mask with one thread
+// per sample and three scalar table loads. Here the reference side of the
+// ratio is a precomputed per-plane table log(max(ref - dark, 1e-5)) (built in
+// FP64 at init), so a sample costs one u16 read, one float table read (the
+// table is L2-resident across a batch) and one float write; the relevant-area
+// mask is a bit mask. The defect repair of the DetectorInterpolation stage
+// can be fused: rows are staged in shared memory, repaired run by run, then
+// converted.
+#include "kernels.h"
+#include "risa_gb300.h"
+
+namespace risa_gb {
+
+namespace {
+constexpr int kThreads = 256;
+constexpr int kRows = 8;        // rows per CTA in the fused-repair path
+constexpr float kClamp = 1e-5f; // the reference's `temp` (Attenuation.cu:144)
+
+__device__ __forceinline__ int frame_plane(int b, int plane, int L) {
+   return plane >= 0 ? plane : (b % L);
+}
+
+__device__ __forceinline__ float atten_one(unsigned raw, float dark, float logden) {
+   float num = __fsub_rn((float)raw, dark);
+   if (num < kClamp) num = kClamp;
+   return __fsub_rn(logden, logf(num));
+}
+
+__device__ __forceinline__ bool mask_keep(const uint32_t* mask, int wpr, int y, int x) {
+   return mask == nullptr || ((__ldg(mask + (size_t)y * wpr + (x >> 5)) >> (x & 31)) & 1u);
+}
+
+// Direct streaming path: each thread converts 8 consecutive samples
+// (one 16-byte u16 load, two 16-byte float stores). Requires D % 8 == 0.
+__global__ void __launch_bounds__(kThreads) attenuation_vec8(const uint16_t* __restrict__ raw,
+                                                             float* __restrict__ out,
+                                                             AttenuationCfg cfg) {
+   const size_t fs = (size_t)cfg.P * cfg.D;
+   const int b = blockIdx.y;
+   const int k = frame_plane(b, cfg.plane, cfg.L);
+   const size_t i8 = ((size_t)blockIdx.x * kThreads + threadIdx.x) * 8;
+   if (i8 >= fs) return;
+   const int y = (int)(i8 / cfg.D), x = (int)(i8 % cfg.D);
+   const uint4 r = __ldg(reinterpret_cast<const uint4*>(raw + (size_t)b * fs + i8));
+   const float4* ld = reinterpret_cast<const float4*>(cfg.logden + (size_t)k * fs + i8);
+   const float4* dk = reinterpret_cast<const float4*>(cfg.dark + (size_t)k * cfg.D + x);
+   const float4 l0 = __ldg(ld), l1 = __ldg(ld + 1);
+   const float4 d0 = __ldg(dk), d1 = __ldg(dk + 1);
+   float v[8];
+   v[0] = atten_one(r.x & 0xFFFFu, d0.x, l0.x);
+   v[1] = atten_one(r.x >> 16, d0.y, l0.y);
+   v[2] = atten_one(r.y & 0xFFFFu, d0.z, l0.z);
+   v[3] = atten_one(r.y >> 16, d0.w, l0.w);
+   v[4] = atten_one(r.z & 0xFFFFu, d1.x, l1.x);
+   v[5] = atten_one(r.z >> 16, d1.y, l1.y);
+   v[6] = atten_one(r.w & 0xFFFFu, d1.z, l1.z);
+   v[7] = atten_one(r.w >> 16, d1.w, l1.w);
+   if (cfg.mask) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+         if (!mask_keep(cfg.mask, cfg.wpr, y, x + j)) v[j] = 0.f;
+   }
+   float4* o = reinterpret_cast<float4*>(out + (size_t)b * fs + i8);
+   __stcs(o, make_float4(v[0], v[1], v[2], v[3]));
+   __stcs(o + 1, make_float4(v[4], v[5], v[6], v[7]));
+}
+
+// Scalar streaming path for any D.
+__global__ void __launch_bounds__(kThreads) attenuation_scalar(const uint16_t* __restrict__ raw,
+                                                               float* __restrict__ out,
+                                                               AttenuationCfg cfg) {
+   const size_t fs = (size_t)cfg.P * cfg.D;
+   const int b = blockIdx.y;
+   const int k = frame_plane(b, cfg.plane, cfg.L);
+   const size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x;
+   if (i >= fs) return;
+   const int y = (int)(i / cfg.D), x = (int)(i % cfg.D);
+   float v = atten_one(__ldg(raw + (size_t)b * fs + i), __ldg(cfg.dark + (size_t)k * cfg.D + x),
+                       __ldg(cfg.logden + (size_t)k * fs + i));
+   if (!mask_keep(cfg.mask, cfg.wpr, y, x)) v = 0.f;
+   out[(size_t)b * fs + i] = v;
+}
+
+// Fused defect repair + attenuation: kRows rows of one frame per CTA.
+__global__ void __launch_bounds__(kThreads) attenuation_repair(const uint16_t* __restrict__ raw,
+                                                               float* __restrict__ out,
+                                                               AttenuationCfg cfg,
+                                                               const int* __restrict__ counts,
+                                                               const DefectRun* __restrict__ runs,
+                                                               int max_runs) {
+   extern __shared__ uint16_t tile[];  // [kRows][D]
+   const int D = cfg.D;
+   const size_t fs = (size_t)cfg.P * D;
+   const int b = blockIdx.y;
+   const int k = frame_plane(b, cfg.plane, cfg.L);
+   const int y0 = blockIdx.x * kRows;
+   const int rows = min(kRows, cfg.P - y0);
+   const uint16_t* src = raw + (size_t)b * fs + (size_t)y0 * D;
+   const int n = rows * D;
+   for (int i = threadIdx.x; i < n; i += kThreads) tile[i] = src[i];
+   __syncthreads();
+   const int nr = counts[b];
+   if (threadIdx.x < rows && nr > 0) {
+      uint16_t* row = tile + threadIdx.x * D;
+      const DefectRun* rl = runs + (size_t)b * max_runs;
+      for (int r = 0; r < nr; ++r) {
+         const DefectRun run = rl[r];
+         for (int m = 0; m < run.len; ++m) {
+            uint16_t val;
+            if (cfg.quirk == RISA_GB_QUIRKS_RISA) {
+               const float w1 = (float)__ddiv_rn((double)m + 1.0, (double)run.len + 1.0);
+               const float w0 = (float)__dsub_rn(1.0, (double)w1);
+               val = (uint16_t)__float2uint_rz(__fadd_rn(__fmul_rn(w0, (float)row[run.left]),
+                                                         __fmul_rn(w1, (float)row[run.right])));
+            } else {
+               const double w1 = __ddiv_rn((double)(m + 1), (double)(run.len + 1));
+               const double w0 = __dsub_rn(1.0, w1);
+               val = (uint16_t)floor(__dadd_rn(__dmul_rn(w0, (double)row[run.left]),
+                                               __dmul_rn(w1, (double)row[run.right])) + 0.5);
+            }
+            row[(run.start + m) % D] = val;
+         }
+      }
+   }
+   __syncthreads();
+   const float* ld = cfg.logden + (size_t)k * fs + (size_t)y0 * D;
+   const float* dk = cfg.dark + (size_t)k * D;
+   float* dst = out + (size_t)b * fs + (size_t)y0 * D;
+   for (int i = threadIdx.x; i < n; i += kThreads) {
+      const int x = i % D;
+      float v = atten_one(tile[i], __ldg(dk + x), __ldg(ld + i));
+      if (!mask_keep(cfg.mask, cfg.wpr, y0 + i / D, x)) v = 0.f;
+      __stcs(dst + i, v);
+   }
+}
+
+// ---- init-time tables ---------------------------------------------------------
+
+// Attenuation::computeAverage (Attenuation.cu:236-251). RISA mode keeps the
+// reference's float accumulation and its (frame + plane) indexing.
+__global__ void reference_average(const uint16_t* __restrict__ frames, int n, int L, int P, int D,
+                                  int quirk, float* __restrict__ avg) {
+   const size_t fs = (size_t)P * D;
+   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   const int k = blockIdx.y;
+   if (i >= fs) return;
+   if (quirk == RISA_GB_QUIRKS_RISA) {
+      const float factor = (float)__ddiv_rn(1.0, (double)(float)n);
+      float acc = 0.f;
+      for (int f = 0; f < n; ++f) acc = __fadd_rn(acc, __fmul_rn((float)frames[(size_t)(f + k) * fs + i], factor));
+      avg[(size_t)k * fs + i] = acc;
+   } else {
+      double acc = 0.0;
+      for (int f = 0; f < n; ++f) acc = __dadd_rn(acc, (double)frames[(size_t)(f * L + k) * fs + i]);
+      avg[(size_t)k * fs + i] = (float)__ddiv_rn(acc, (double)n);
+   }
+}
+
+// Attenuation::computeDarkAverage (Attenuation.cu:219-234); RISA mode's
+// factor is 0, so its dark average is identically zero.
+__global__ void dark_average(const uint16_t* __restrict__ frames, int n, int L, int P, int D,
+                             int quirk, float* __restrict__ dark) {
+   const int d = blockIdx.x * blockDim.x + threadIdx.x;
+   const int k = blockIdx.y;
+   if (d >= D) return;
+   if (quirk == RISA_GB_QUIRKS_RISA) {
+      dark[k * D + d] = 0.f;
+      return;
+   }
+   const size_t fs = (size_t)P * D;
+   double acc = 0.0;
+   for (int f = 0; f < n; ++f)
+      for (int p = 0; p < P; ++p) acc = __dadd_rn(acc, (double)frames[(size_t)(f * L + k) * fs + (size_t)p * D + d]);
+   dark[k * D + d] = (float)__ddiv_rn(acc, __dmul_rn((double)n, (double)P));
+}
+
+__global__ void logden_table(const float* __restrict__ avg, const float* __restrict__ dark, int P,
+                             int D, float* __restrict__ logden) {
+   const size_t fs = (size_t)P * D;
+   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   const int k = blockIdx.y;
+   if (i >= fs) return;
+   float den = __fsub_rn(avg[(size_t)k * fs + i], dark[(size_t)k * D + i % D]);
+   if (den < kClamp) den = kClamp;
+   logden[(size_t)k * fs + i] = (float)log((double)den);
+}
+}  // namespace
+
+cudaError_t launch_attenuation(const uint16_t* raw, float* out, int batch,
+                               const AttenuationCfg& cfg, const DefectWorkspace* runs,
+                               int max_runs, cudaStream_t st) {
+   if (batch <= 0) return cudaSuccess;
+   const size_t fs = (size_t)cfg.P * cfg.D;
+   if (runs) {
+      const size_t smem = sizeof(uint16_t) * kRows * cfg.D;
+      if (smem > 48 * 1024) {
+         cudaError_t e = cudaFuncSetAttribute(attenuation_repair,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+         if (e != cudaSuccess) return e;
+      }
+      dim3 grid((cfg.P + kRows - 1) / kRows, batch);
+      attenuation_repair<<<grid, kThreads, smem, st>>>(raw, out, cfg, runs->counts, runs->runs,
+                                                       max_runs);
+   } else if (cfg.D % 8 == 0) {
+      dim3 grid((unsigned)((fs / 8 + kThreads - 1) / kThreads), batch);
+      attenuation_vec8<<<grid, kThreads, 0, st>>>(raw, out, cfg);
+   } else {
+      dim3 grid((unsigned)((fs + kThreads - 1) / kThreads), batch);
+      attenuation_scalar<<<grid, kThreads, 0, st>>>(raw, out, cfg);
+   }
+   return cudaGetLastError();
+}
+
+cudaError_t launch_reference_average(const uint16_t* frames, int n, int L, int P, int D, int quirk,
+                                     float* avg, cudaStream_t st) {
+   const size_t fs = (size_t)P * D;
+   dim3 grid((unsigned)((fs + 255) / 256), L);
+   reference_average<<<grid, 256, 0, st>>>(frames, n, L, P, D, quirk, avg);
+   return cudaGetLastError();
+}
+
+cudaError_t launch_dark_average(const uint16_t* frames, int n, int L, int P, int D, int quirk,
+                                float* dark, cudaStream_t st) {
+   dim3 grid((D + 127) / 128, L);
+   dark_average<<<grid, 128, 0, st>>>(frames, n, L, P, D, quirk, dark);
+   return cudaGetLastError();
+}
+
+cudaError_t launch_logden(const float* avg, const float* dark, int L, int P, int D, float* logden,
+                          cudaStream_t st) {
+   const size_t fs = (size_t)P * D;
+   dim3 grid((unsigned)((fs + 255) / 256), L);
+   logden_table<<<grid, 256, 0, st>>>(avg, dark, P, D, logden);
+   return cudaGetLastError();
+}
+
+}  // namespace risa_gb

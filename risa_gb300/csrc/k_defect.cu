@@ -1,0 +1,250 @@
+// Detector-defect detection and repair on the device.
+//
+// The reference runs this on the host with a device->host->device round trip
+// per frame (DetectorInterpolation.cu:113-139) using findDefectDetectors and
+// interpolateDefectDetectors (interpolationFunctions.h:28-97). Here:
+//   1. defect_stats: per-column total variation (exact integer sum, so the
+//      result does not depend on the reduction order) and max/min, reduced
+//      over row chunks with integer atomics;
+//   2. defect_flags: one CTA per frame forms var = TV * range^2 in FP64,
+//      applies the 17-tap threshold with the reference's exact operation
+//      order (no FMA contraction) and compiles the ordered list of defect
+//      runs;
+//   3. defect_repair (or the attenuation kernel, fused): each row applies the
+//      runs in list order, so in-place dependencies between runs resolve as
+//      in the reference's sequential loop.
+#include "kernels.h"
+#include "risa_gb300.h"
+
+namespace risa_gb {
+
+namespace {
+constexpr int kStatThreads = 128;
+constexpr int kStatRows = 128;
+__constant__ double c_defect_filter[9];
+
+__global__ void defect_stats_init(ColStats* st, int n) {
+   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) {
+      st[i].tv = 0ull;
+      st[i].mx = 0u;
+      st[i].mn = 0xFFFFu;
+   }
+}
+
+// grid: x = column blocks, y = row chunks, z = frame. One thread per column.
+__global__ void __launch_bounds__(kStatThreads) defect_stats(const uint16_t* __restrict__ frames,
+                                                             ColStats* __restrict__ st, int P,
+                                                             int D) {
+   const int d = blockIdx.x * kStatThreads + threadIdx.x;
+   if (d >= D) return;
+   const int r0 = blockIdx.y * kStatRows;
+   const int r1 = min(r0 + kStatRows, P - 1);  // pairs (p, p+1) with p <= P-2
+   if (r0 >= r1) return;
+   const uint16_t* f = frames + (size_t)blockIdx.z * P * D + d;
+   unsigned int prev = __ldg(f + (size_t)r0 * D);
+   unsigned int mx = prev, mn = prev;
+   unsigned long long tv = 0ull;
+#pragma unroll 8
+   for (int p = r0; p < r1; ++p) {
+      const unsigned int next = __ldg(f + (size_t)(p + 1) * D);
+      tv += (prev > next) ? (prev - next) : (next - prev);
+      mx = max(mx, prev);
+      mn = min(mn, prev);
+      prev = next;
+   }
+   ColStats* s = st + (size_t)blockIdx.z * D + d;
+   atomicAdd(&s->tv, tv);
+   atomicMax(&s->mx, mx);
+   atomicMin(&s->mn, mn);
+}
+
+// One CTA per frame. Dynamic shared memory: var[D] (double) then flags[D+1].
+__global__ void defect_flags(const ColStats* __restrict__ st, DefectCfg cfg,
+                             int32_t* __restrict__ flags_out, int* __restrict__ counts,
+                             DefectRun* __restrict__ runs) {
+   extern __shared__ double smem_d[];
+   const int D = cfg.D;
+   double* var = smem_d;
+   int* flags = reinterpret_cast<int*>(var + D);
+   const int f = blockIdx.x;
+   const ColStats* s = st + (size_t)f * D;
+   for (int d = threadIdx.x; d < D; d += blockDim.x) {
+      const unsigned long long range = (unsigned long long)(s[d].mx - s[d].mn);
+      var[d] = __dmul_rn((double)s[d].tv, (double)(range * range));
+      flags[d] = 0;
+   }
+   if (threadIdx.x == 0) flags[D] = 0;
+   __syncthreads();
+   const unsigned H = (unsigned)D / 2u;
+   for (unsigned t = threadIdx.x; t < 2u * H; t += blockDim.x) {
+      const unsigned seg = t / H, i = t % H;
+      double th = 0.0;
+#pragma unroll
+      for (unsigned j = 0; j < 9u; ++j) {
+         unsigned i1;
+         if (cfg.quirk == RISA_GB_QUIRKS_RISA)
+            i1 = (i - j) % H;  // unsigned wrap, interpolationFunctions.h:53
+         else
+            i1 = (i + H * 9u - j) % H;
+         const unsigned i2 = (i + j) % H;
+         th = __dadd_rn(th, __dmul_rn(c_defect_filter[j], var[i1 + seg * H]));
+         th = __dadd_rn(th, __dmul_rn(c_defect_filter[j], var[i2 + seg * H]));
+      }
+      const unsigned det = seg * H + i;
+      if (var[det] < __dmul_rn(cfg.thresh_min, th)) flags[det] = 1;
+      if (var[det] > __dmul_rn(cfg.thresh_max, th)) {
+         for (int off = -2; off <= 2; ++off) {
+            unsigned k;
+            if (cfg.quirk == RISA_GB_QUIRKS_RISA)
+               k = (det + (unsigned)off) % (unsigned)D;
+            else
+               k = (det + (unsigned)D + (unsigned)off) % (unsigned)D;
+            flags[k] = 1;
+         }
+      }
+   }
+   __syncthreads();
+   if (flags_out)
+      for (int d = threadIdx.x; d < D; d += blockDim.x) flags_out[(size_t)f * D + d] = flags[d];
+   if (threadIdx.x != 0) return;
+
+   // Ordered run list (single thread; a handful of runs per frame).
+   DefectRun* out = runs + (size_t)f * cfg.max_runs;
+   int n = 0;
+   const unsigned uD = (unsigned)D;
+   if (cfg.quirk == RISA_GB_QUIRKS_RISA) {
+      // interpolationFunctions.h:76-96: flags[D] reads as 0
+      unsigned det = 0;
+      while (det < uD) {
+         if (flags[det]) {
+            const unsigned det0 = det;
+            while (flags[det] && flags[(det + 1u) % uD]) det++;
+            if (n < cfg.max_runs) {
+               DefectRun r;
+               r.start = (uint16_t)det0;
+               r.len = (uint16_t)(det - det0 + 1u);
+               r.left = (uint16_t)((det0 - 1u) % uD);
+               r.right = (uint16_t)((det + 1u) % uD);
+               out[n] = r;
+            }
+            ++n;
+         }
+         det++;
+      }
+   } else {
+      unsigned start = uD;
+      for (unsigned d = 0; d < uD; ++d)
+         if (!flags[d]) { start = d; break; }
+      if (start < uD) {
+         unsigned k = 1;
+         while (k <= uD) {
+            const unsigned d = (start + k) % uD;
+            if (!flags[d]) { ++k; continue; }
+            unsigned len = 0;
+            while (flags[(start + k + len) % uD]) ++len;
+            if (n < cfg.max_runs) {
+               DefectRun r;
+               r.start = (uint16_t)d;
+               r.len = (uint16_t)len;
+               r.left = (uint16_t)((start + k - 1u) % uD);
+               r.right = (uint16_t)((start + k + len) % uD);
+               out[n] = r;
+            }
+            ++n;
+            k += len;
+         }
+      }
+   }
+   counts[f] = n < cfg.max_runs ? n : cfg.max_runs;
+}
+
+__global__ void defect_repair(uint16_t* __restrict__ frames, DefectCfg cfg,
+                              const int* __restrict__ counts, const DefectRun* __restrict__ runs) {
+   const int p = blockIdx.x * blockDim.x + threadIdx.x;
+   const int f = blockIdx.y;
+   if (p >= cfg.P) return;
+   const int n = counts[f];
+   uint16_t* row = frames + ((size_t)f * cfg.P + p) * cfg.D;
+   const DefectRun* rl = runs + (size_t)f * cfg.max_runs;
+   for (int r = 0; r < n; ++r) {
+      const DefectRun run = rl[r];
+      for (int m = 0; m < run.len; ++m) {
+         const int col = (run.start + m) % cfg.D;
+         uint16_t val;
+         if (cfg.quirk == RISA_GB_QUIRKS_RISA) {
+            const float w1 = (float)__ddiv_rn((double)m + 1.0, (double)run.len + 1.0);
+            const float w0 = (float)__dsub_rn(1.0, (double)w1);
+            const float v = __fadd_rn(__fmul_rn(w0, (float)row[run.left]),
+                                      __fmul_rn(w1, (float)row[run.right]));
+            val = (uint16_t)__float2uint_rz(v);
+         } else {
+            const double w1 = __ddiv_rn((double)(m + 1), (double)(run.len + 1));
+            const double w0 = __dsub_rn(1.0, w1);
+            const double v = __dadd_rn(__dmul_rn(w0, (double)row[run.left]),
+                                       __dmul_rn(w1, (double)row[run.right]));
+            val = (uint16_t)floor(v + 0.5);
+         }
+         row[col] = val;
+      }
+   }
+}
+}  // namespace
+
+size_t defects_workspace_bytes(int D, int batch, int max_runs) {
+   auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+   return align(sizeof(ColStats) * (size_t)D * batch) + align(sizeof(int) * (size_t)batch) +
+          align(sizeof(DefectRun) * (size_t)max_runs * batch);
+}
+
+DefectWorkspace defects_carve(void* ws, int D, int batch, int max_runs) {
+   auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+   char* p = static_cast<char*>(ws);
+   DefectWorkspace w;
+   w.stats = reinterpret_cast<ColStats*>(p);
+   p += align(sizeof(ColStats) * (size_t)D * batch);
+   w.counts = reinterpret_cast<int*>(p);
+   p += align(sizeof(int) * (size_t)batch);
+   w.runs = reinterpret_cast<DefectRun*>(p);
+   (void)max_runs;
+   return w;
+}
+
+cudaError_t upload_defect_filter(cudaStream_t st) {
+   // Attenuation.cu:179-182: the 17-tap kernel scaled by (1/sum); taps 0..8 are used.
+   static const double raw[17] = {0.5, 1.0, 1.0, 1.0, 1.5, 2.0, 3.0, 3.5, 2.0,
+                                  3.5, 3.0, 2.0, 1.5, 1.0, 1.0, 1.0, 0.5};
+   double sum = 0.0;
+   for (double v : raw) sum += v;
+   const double inv = 1.0 / sum;
+   double f[9];
+   for (int i = 0; i < 9; ++i) f[i] = inv * raw[i];
+   // up to 8192 columns: var (8 B) + flags (4 B) per column
+   cudaError_t e = cudaFuncSetAttribute(defect_flags, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        8192 * 12 + 64);
+   if (e != cudaSuccess) return e;
+   return cudaMemcpyToSymbolAsync(c_defect_filter, f, sizeof(f), 0, cudaMemcpyHostToDevice, st);
+}
+
+cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const DefectCfg& cfg,
+                                 DefectWorkspace ws, int32_t* flags_out, cudaStream_t st) {
+   if (batch <= 0) return cudaSuccess;
+   const int n = cfg.D * batch;
+   defect_stats_init<<<(n + 255) / 256, 256, 0, st>>>(ws.stats, n);
+   dim3 grid((cfg.D + kStatThreads - 1) / kStatThreads, (cfg.P - 1 + kStatRows - 1) / kStatRows,
+             batch);
+   defect_stats<<<grid, kStatThreads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D);
+   const size_t smem = sizeof(double) * cfg.D + sizeof(int) * (cfg.D + 1);
+   defect_flags<<<batch, 256, smem, st>>>(ws.stats, cfg, flags_out, ws.counts, ws.runs);
+   return cudaGetLastError();
+}
+
+cudaError_t launch_defect_repair(uint16_t* frames, int batch, const DefectCfg& cfg,
+                                 DefectWorkspace ws, cudaStream_t st) {
+   if (batch <= 0) return cudaSuccess;
+   dim3 grid((cfg.P + 127) / 128, batch);
+   defect_repair<<<grid, 128, 0, st>>>(frames, cfg, ws.counts, ws.runs);
+   return cudaGetLastError();
+}
+
+}  // namespace risa_gb

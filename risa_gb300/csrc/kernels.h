@@ -1,0 +1,124 @@
+// Launch wrappers of the sm_103a kernels (one .cu file per stage). All take
+// device pointers, never allocate, and report launch errors through the
+// returned cudaError_t.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace risa_gb {
+
+// ---------------------------------------------------------------- defects
+// Per-column statistics of one frame (interpolationFunctions.h:36-47):
+// total variation over consecutive projections (exact integer sum) and the
+// max/min over projections 0..P-2.
+struct ColStats {
+   unsigned long long tv;
+   unsigned int mx;
+   unsigned int mn;
+};
+// One run of defect columns, processed in list order: columns
+// start .. start+len-1 (taken modulo D when written), repaired from `left`
+// and `right` with weights (m+1)/(len+1).
+struct DefectRun {
+   uint16_t start, len, left, right;
+};
+struct DefectCfg {
+   int P, D;
+   double thresh_min, thresh_max;
+   int quirk;
+   int max_runs;  // per frame (D/2 + 2)
+};
+size_t defects_workspace_bytes(int D, int batch, int max_runs);
+// Workspace layout: [batch*D ColStats][batch int run counts][batch*max_runs DefectRun]
+struct DefectWorkspace {
+   ColStats* stats;
+   int* counts;
+   DefectRun* runs;
+};
+DefectWorkspace defects_carve(void* ws, int D, int batch, int max_runs);
+cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const DefectCfg& cfg,
+                                 DefectWorkspace ws, int32_t* flags_out, cudaStream_t st);
+cudaError_t launch_defect_repair(uint16_t* frames, int batch, const DefectCfg& cfg,
+                                 DefectWorkspace ws, cudaStream_t st);
+// Sets the 9 normalised smoothing weights (defect threshold) for this device.
+cudaError_t upload_defect_filter(cudaStream_t st);
+
+// ---------------------------------------------------------------- attenuation
+struct AttenuationCfg {
+   int P, D, L;
+   int plane;             // >= 0 fixed plane, -1 interleaved (frame b -> plane b % L)
+   const float* logden;   // [L][P][D] log(max(ref - dark, 1e-5))
+   const float* dark;     // [L][D]
+   const uint32_t* mask;  // relevant-area bits [P][wpr] or nullptr
+   int wpr;
+   int quirk;
+};
+// With runs != nullptr the defect repair of each frame is applied on the fly.
+cudaError_t launch_attenuation(const uint16_t* raw, float* out, int batch,
+                               const AttenuationCfg& cfg, const DefectWorkspace* runs,
+                               int max_runs, cudaStream_t st);
+// Reference-frame tables: avg [L][P][D] float from [n][L][P][D] u16 frames.
+cudaError_t launch_reference_average(const uint16_t* frames, int n_frames, int L, int P, int D,
+                                     int quirk, float* avg, cudaStream_t st);
+cudaError_t launch_dark_average(const uint16_t* frames, int n_frames, int L, int P, int D,
+                                int quirk, float* dark, cudaStream_t st);
+cudaError_t launch_logden(const float* avg, const float* dark, int L, int P, int D,
+                          float* logden, cudaStream_t st);
+
+// ---------------------------------------------------------------- fan2para
+struct F2PCfg {
+   int Pf, Df, Pp, Dp, L;
+   int plane;               // >= 0 fixed plane, -1 interleaved
+   const uint32_t* packed;  // [L][4][Pp*Dp]
+   const float* u;          // [L][4][Pp*Dp]
+   const float* v;          // [L][4][Pp*Dp]
+};
+cudaError_t launch_fan2para(const float* fan, float* par, int batch, const F2PCfg& cfg,
+                            cudaStream_t st);
+// Transpose of the rebinning through a CSR table over fan samples.
+struct F2PAdjCfg {
+   int Pf, Df, Pp, Dp, L;
+   int plane;
+   const int* row_ptr;   // [L][Pf*Df + 1]
+   const int* col;       // parallel sample index
+   const float* w;       // weights
+   int nnz_stride;       // entries per plane in col/w
+};
+cudaError_t launch_fan2para_adjoint(const float* par, float* fan, int batch, const F2PAdjCfg& cfg,
+                                    cudaStream_t st);
+
+// ---------------------------------------------------------------- filter
+struct FilterCfg {
+   int rows, Dp, len;
+   const float2* twiddle;  // [len/2] exp(-2 pi i k / len)
+   const float* h;         // [len/2 + 1]
+};
+cudaError_t launch_filter(float* sino, int batch, const FilterCfg& cfg, cudaStream_t st);
+
+// ---------------------------------------------------------------- backprojection
+struct BPCfg {
+   int Pp, Dp, N;
+   const float* a;      // [Pp]
+   const float* b;      // [Pp]
+   const double* ad;    // [Pp] FP64 copies of a and b
+   const double* bd;    // [Pp]
+   const double* t0;    // [Pp]
+   float norm;
+   int masking;         // fused inscribed-circle mask
+   float mask_value;
+   int interp;          // RISA_GB_INTERP_*
+   float scale;         // Dp / N (bins per pixel)
+};
+int bp_variant_count();
+const char* bp_variant_name(int v);
+cudaError_t launch_backprojection(const float* sino, float* img, int batch, const BPCfg& cfg,
+                                  int variant, cudaStream_t st);
+cudaError_t launch_backprojection_adjoint(const float* img, float* sino, int batch,
+                                          const BPCfg& cfg, cudaStream_t st);
+
+// ---------------------------------------------------------------- masking
+cudaError_t launch_mask(float* img, int batch, int N, float value, int normalize,
+                        float* ws_minmax, int masking, cudaStream_t st);
+
+}  // namespace risa_gb

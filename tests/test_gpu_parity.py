@@ -1,0 +1,325 @@
+"""GPU parity: every stage through the C ABI against the CPU oracle.
+
+Index work (defect flags, repaired uint16 frames, averaged tables) must match
+bit for bit. FP32 outputs are compared with
+    max_rel = max|gpu - oracle| / max|oracle|      (<= 1e-5, the FP32 bar)
+    rel_l2  = ||gpu - oracle||_2 / ||oracle||_2
+against the FP64 oracle run on the same inputs.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import risa_gb300 as rg
+from risa_gb300 import phantom
+from tests.helpers import ROFEX, SMALL, geom, ns, rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+MAX_REL = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.init()
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+# ------------------------------------------------------------------------------ defects
+@pytest.mark.parametrize("quirk", [rg.QUIRKS_RISA, rg.QUIRKS_NONE])
+def test_defects_bit_exact(golden_dir, quirk):
+    d = np.load(os.path.join(golden_dir, "defects.npz"))
+    for name in ("mid", "wrap", "all_edges", "clean"):
+        frame = d[f"{name}_frame"]
+        P, D = frame.shape
+        tmin, tmax = d[f"{name}_thresh"]
+        g = rg.make_geometry(n_fan_det=D, n_fan_proj=P)
+        p = rg.make_params(quirks=quirk, thresh_min=tmin, thresh_max=tmax)
+        h = rg.Defects(g, p, max_batch=3)
+        frames = np.stack([frame, frame[::-1].copy(), frame])
+        t = dev(frames.view(np.int16))
+        ws = torch.empty(h.workspace_bytes(3), dtype=torch.uint8, device="cuda")
+        flags = torch.zeros((3, D), dtype=torch.int32, device="cuda")
+        h.enqueue(t, 3, ws, flags_out=flags)
+        got = host(t).view(np.uint16)
+        gf = host(flags)
+        for b in range(3):
+            of = oracle.find_defects(frames[b], tmin, tmax, quirk)
+            np.testing.assert_array_equal(gf[b], of[:D], err_msg=f"{name} flags {b}")
+            np.testing.assert_array_equal(got[b], oracle.interpolate_defects(frames[b], of, quirk),
+                                          err_msg=f"{name} frame {b}")
+        if quirk == rg.QUIRKS_RISA:  # and against the reference's own output
+            np.testing.assert_array_equal(got[0], d[f"{name}_repaired"])
+
+
+def test_defects_on_scan_frames():
+    sc = phantom.make_scan(2, 1, 200, 432, 215.0, 240.0, seed=3, defect_fraction=0.02, distinct=2)
+    g = rg.make_geometry(n_fan_det=432, n_fan_proj=200)
+    for quirk in (rg.QUIRKS_RISA, rg.QUIRKS_NONE):
+        h = rg.Defects(g, rg.make_params(quirks=quirk), max_batch=2)
+        t = dev(sc.raw.view(np.int16))
+        ws = torch.empty(h.workspace_bytes(2), dtype=torch.uint8, device="cuda")
+        h.enqueue(t, 2, ws)
+        got = host(t).view(np.uint16)
+        for b in range(2):
+            of = oracle.find_defects(sc.raw[b], 0.67, 1.5, quirk)
+            assert of[sc.dead].all()
+            np.testing.assert_array_equal(got[b], oracle.interpolate_defects(sc.raw[b], of, quirk))
+
+
+# ------------------------------------------------------------------------------ attenuation
+@pytest.mark.parametrize("quirk", [rg.QUIRKS_RISA, rg.QUIRKS_NONE])
+def test_attenuation(quirk):
+    d = dict(SMALL, n_planes=2, source_diameter=[430.0, 430.0], delta_x=[0, 0], delta_z=[1417, 1430],
+             source_angle=[360, 360])
+    sc = phantom.make_scan(3, 2, 500, 432, 215.0, 240.0, seed=5, defect_fraction=0.01, distinct=3)
+    g = geom(d)
+    p = rg.make_params(quirks=quirk)
+    att = rg.Attenuation(g, p, sc.ref, 1, sc.dark, 1)
+    ref_t, dark_t = att.tables()
+    oref, odark = oracle.attenuation_init(sc.ref, sc.dark, 2, 0.67, 1.5, True, quirk)
+    np.testing.assert_array_equal(ref_t.view(np.uint32), oref.view(np.uint32))
+    np.testing.assert_array_equal(dark_t.view(np.uint32), odark.view(np.uint32))
+    raw = dev(sc.raw.view(np.int16))
+    out = torch.empty(sc.raw.shape, dtype=torch.float32, device="cuda")
+    att.enqueue(raw, out, rg.PLANES_INTERLEAVED, sc.raw.shape[0])
+    got = host(out)
+    for b in range(sc.raw.shape[0]):
+        k = b % 2
+        exp = oracle.attenuation(sc.raw[b], oref[k], odark[k])
+        mr, _ = rel_err(got[b], exp)
+        assert mr < MAX_REL, (b, mr)
+
+
+def test_attenuation_relevant_mask():
+    g = geom(ROFEX)
+    p = rg.make_params(quirks=rg.QUIRKS_RISA, relevant_mask=True, lower_lim_offset=47.0,
+                       upper_lim_offset=313.0, fix_points=(43, 285, 175, 362, 0, 431))
+    rng = np.random.default_rng(0)
+    ref = rng.integers(30000, 40000, size=(2, 500, 432)).astype(np.uint16)
+    raw = rng.integers(1000, 30000, size=(2, 500, 432)).astype(np.uint16)
+    att = rg.Attenuation(g, p, ref, 1, None, 0)
+    oref, odark = oracle.attenuation_init(ref, None, 2, 0.67, 1.5, True, rg.QUIRKS_RISA)
+    mask = oracle.relevant_area_mask(432, 500, 23.2, 47.0, 313.0, 43, 285, 175, 362, 0, 431)
+    out = torch.empty((2, 500, 432), dtype=torch.float32, device="cuda")
+    att.enqueue(dev(raw.view(np.int16)), out, 1, 2)
+    got = host(out)
+    for b in range(2):
+        exp = oracle.attenuation(raw[b], oref[1], odark[1], mask)
+        assert np.all(got[b][mask == 0] == 0)
+        assert rel_err(got[b], exp)[0] < MAX_REL
+
+
+# ------------------------------------------------------------------------------ fan2para
+@pytest.mark.parametrize("quirk", [rg.QUIRKS_RISA, rg.QUIRKS_NONE])
+@pytest.mark.parametrize("gname", ["small", "rofex"])
+def test_fan2para(quirk, gname):
+    d = SMALL if gname == "small" else ROFEX
+    g = geom(d)
+    f2p = rg.Fan2Para(g, rg.make_params(quirks=quirk))
+    rec = oracle.f2p_records(ns(d), quirk)
+    L = d["n_planes"]
+    B = 5
+    rng = np.random.default_rng(1)
+    fan = rng.standard_normal((B, d["n_fan_proj"], d["n_fan_det"])).astype(np.float32)
+    par = torch.empty((B, d["n_par_proj"], d["n_par_det"]), dtype=torch.float32, device="cuda")
+    for plane in ([rg.PLANES_INTERLEAVED] if L > 1 else []) + list(range(L)):
+        f2p.enqueue(dev(fan), par, plane, B)
+        got = host(par)
+        for b in range(B):
+            k = plane if plane >= 0 else b % L
+            exp = oracle.f2p_apply(rec, k, quirk, fan[b])
+            mr, _ = rel_err(got[b], exp)
+            assert mr < MAX_REL, (plane, b, mr)
+
+
+# ------------------------------------------------------------------------------ filter
+@pytest.mark.parametrize("dp,pad,quirk,ftype", [
+    (64, 0, rg.QUIRKS_RISA, "ramp"), (256, 0, rg.QUIRKS_NONE, "sheppLogan"),
+    (1024, 0, rg.QUIRKS_NONE, "sheppLogan"), (160, 0, rg.QUIRKS_NONE, "hanning"),
+    (1024, 0, rg.QUIRKS_RISA, "hamming"), (768, 0, rg.QUIRKS_NONE, "ramp"),
+    (2048, 0, rg.QUIRKS_NONE, "cosine"), (4000, 0, rg.QUIRKS_NONE, "ramp")])
+def test_filter(dp, pad, quirk, ftype):
+    rows = 37
+    g = rg.make_geometry(n_par_proj=rows, n_par_det=dp, n_pixels=64)
+    p = rg.make_params(quirks=quirk, filter_type=ftype, pad=pad, cutoff=0.9)
+    filt = rg.Filter(g, p)
+    n, h = filt.response()
+    rng = np.random.default_rng(dp)
+    x = np.abs(rng.standard_normal((2, rows, dp))).astype(np.float32)
+    t = dev(x)
+    filt.enqueue(t, 2)
+    got = host(t)
+    ho = oracle.design_filter(n, rg.FILTERS[ftype], 0.9, quirk)
+    for b in range(2):
+        exp = oracle.filter_rows(x[b], n, ho)
+        mr, l2 = rel_err(got[b], exp)
+        assert mr < MAX_REL, (b, mr)
+
+
+# ------------------------------------------------------------------------------ backprojection
+@pytest.mark.parametrize("quirk", [rg.QUIRKS_RISA, rg.QUIRKS_NONE])
+@pytest.mark.parametrize("interp", [rg.INTERP_LINEAR, rg.INTERP_NEAREST, rg.INTERP_NEAREST_TRUNC])
+def test_backprojection(quirk, interp):
+    Pp, Dp, N = 90, 128, 96
+    g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=N, rotation_offset=-7.5)
+    p = rg.make_params(quirks=quirk, interp=interp)
+    bp = rg.Backprojection(g, p)
+    sino, _ = phantom.parallel_sinograms(2, Pp, Dp, 200.0, seed=4)
+    img = torch.empty((2, N, N), dtype=torch.float32, device="cuda")
+    for v in range(rg.Backprojection.variant_count()):
+        bp.set_variant(v)
+        bp.enqueue(dev(sino), img, 2)
+        got = host(img)
+        for b in range(2):
+            exp = oracle.backproject(sino[b], N, -7.5, interp, quirk)
+            mr, _ = rel_err(got[b], exp)
+            tol = MAX_REL if interp == rg.INTERP_LINEAR else 2e-3  # nearest: exact .5 ties may round apart
+            assert mr < tol, (v, b, mr)
+
+
+def test_backprojection_masking_and_autotune():
+    Pp, Dp, N = 128, 160, 128
+    g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=N)
+    p = rg.make_params(masking=True, masking_value=-1.0)
+    bp = rg.Backprojection(g, p)
+    sino, _ = phantom.parallel_sinograms(3, Pp, Dp, 200.0, seed=9)
+    img = torch.empty((3, N, N), dtype=torch.float32, device="cuda")
+    v = bp.autotune(dev(sino), img, 3)
+    assert 0 <= v < rg.Backprojection.variant_count()
+    bp.enqueue(dev(sino), img, 3)
+    got = host(img)
+    for b in range(3):
+        exp = oracle.mask(oracle.backproject(sino[b], N), -1.0)
+        assert rel_err(got[b], exp)[0] < MAX_REL
+        yy, xx = np.mgrid[:N, :N]
+        out = (xx - (N - 1) / 2) ** 2 + (yy - (N - 1) / 2) ** 2 > N * N / 4
+        assert np.all(got[b][out] == -1.0)
+
+
+def test_masking_normalisation():
+    N = 64
+    g = rg.make_geometry(n_pixels=N, n_par_proj=8, n_par_det=8)
+    m = rg.Masking(g, rg.make_params(masking=True, normalize=True, masking_value=0.5))
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((2, N, N)).astype(np.float32)
+    t = dev(x)
+    ws = torch.empty(m.workspace_bytes(2), dtype=torch.uint8, device="cuda")
+    m.enqueue(t, 2, ws)
+    got = host(t)
+    for b in range(2):
+        assert rel_err(got[b], oracle.mask(x[b], 0.5, True))[0] < 1e-6
+
+
+# ------------------------------------------------------------------------------ whole chain
+def _fbp_case(quirk, defects, masking, L=1, frames=3):
+    d = dict(SMALL, n_planes=L, source_diameter=[430.0] * L, delta_x=[0.0] * L,
+             delta_z=[1417.0 + 13 * k for k in range(L)], source_angle=[360.0] * L,
+             n_par_proj=96, n_par_det=96, n_pixels=96)
+    sc = phantom.make_scan(frames, L, 500, 432, 215.0, 240.0, seed=11, defect_fraction=0.01 if defects else 0,
+                           distinct=frames)
+    ftype = "sheppLogan"
+    g = geom(d)
+    p = rg.make_params(quirks=quirk, filter_type=ftype, defects=defects, masking=masking)
+    op = oracle.make_params(quirk=quirk, filter_type=ftype, defects=defects, masking=masking)
+    return d, sc, g, p, op
+
+
+@pytest.mark.parametrize("quirk", [rg.QUIRKS_NONE, rg.QUIRKS_RISA])
+@pytest.mark.parametrize("defects", [False, True])
+def test_fbp_chain_vs_oracle(quirk, defects):
+    d, sc, g, p, op = _fbp_case(quirk, defects, masking=True, L=2)
+    n = sc.raw.shape[0]
+    fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=n)
+    img = torch.empty((n, d["n_pixels"], d["n_pixels"]), dtype=torch.float32, device="cuda")
+    fbp.enqueue(dev(sc.raw.view(np.int16)), img, rg.PLANES_INTERLEAVED, n)
+    got = host(img)
+    oref, odark = oracle.attenuation_init(sc.ref, sc.dark, 2, 0.67, 1.5, True, quirk)
+    rec = oracle.f2p_records(ns(d), quirk)
+    exp = oracle.fbp(ns(d), op, rec, oref, odark, sc.raw, sc.planes)
+    for b in range(n):
+        mr, l2 = rel_err(got[b], exp[b])
+        assert mr < MAX_REL and l2 < MAX_REL, (b, mr, l2)
+
+
+def test_graph_replay_and_host_path_match_enqueue():
+    d, sc, g, p, op = _fbp_case(rg.QUIRKS_NONE, True, True, L=2, frames=4)
+    n = sc.raw.shape[0]  # 8 frames
+    B = 4
+    fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=B)
+    N = d["n_pixels"]
+    raw = dev(sc.raw.view(np.int16))
+    ref_img = torch.empty((n, N, N), dtype=torch.float32, device="cuda")
+    for c in range(0, n, B):
+        fbp.enqueue(raw[c:c + B], ref_img[c:c + B], rg.PLANES_INTERLEAVED, B)
+    expect = host(ref_img)
+    s = torch.cuda.Stream()
+    img = torch.zeros((n, N, N), dtype=torch.float32, device="cuda")
+    graph = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, s)
+    assert graph.kernel_count >= 2 * 5  # two chunks of the chain
+    graph.replay(s)
+    s.synchronize()
+    np.testing.assert_array_equal(img.cpu().numpy(), expect)
+    hraw = torch.from_numpy(sc.raw.view(np.int16)).pin_memory()
+    himg = torch.zeros((n, N, N), dtype=torch.float32).pin_memory()
+    fbp.run_host(hraw, himg, n, rg.PLANES_INTERLEAVED)
+    np.testing.assert_array_equal(himg.numpy(), expect)
+    # a ragged tail (n not a multiple of the batch) goes through the direct path
+    himg2 = torch.zeros((n - 2, N, N), dtype=torch.float32).pin_memory()
+    fbp.run_host(hraw[: n - 2], himg2, n - 2, rg.PLANES_INTERLEAVED)
+    np.testing.assert_array_equal(himg2.numpy(), expect[: n - 2])
+
+
+def test_errors_are_reported():
+    g = rg.make_geometry(n_par_proj=16, n_par_det=16, n_pixels=16)
+    bp = rg.Backprojection(g, rg.make_params())
+    with pytest.raises(rg.RisaError) as e:
+        bp.enqueue(0, 0, 1)
+    assert e.value.status == -1
+    with pytest.raises(rg.RisaError):
+        rg.Fan2Para(rg.make_geometry(n_planes=0), rg.make_params())
+
+
+# ------------------------------------------------------------------------------ adjoints
+def test_backprojection_adjoint_dot_product():
+    Pp, Dp, N = 60, 80, 64
+    g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=N)
+    bp = rg.Backprojection(g, rg.make_params())
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((2, Pp, Dp)).astype(np.float32)
+    y = rng.standard_normal((2, N, N)).astype(np.float32)
+    ax = torch.empty((2, N, N), dtype=torch.float32, device="cuda")
+    aty = torch.empty((2, Pp, Dp), dtype=torch.float32, device="cuda")
+    bp.enqueue(dev(x), ax, 2)
+    bp.enqueue_adjoint(dev(y), aty, 2)
+    lhs = float((host(ax).astype(np.float64) * y).sum())
+    rhs = float((x.astype(np.float64) * host(aty)).sum())
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
+
+
+def test_fan2para_adjoint_dot_product():
+    g = geom(SMALL)
+    f2p = rg.Fan2Para(g, rg.make_params())
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((1, 500, 432)).astype(np.float32)
+    y = rng.standard_normal((1, 64, 64)).astype(np.float32)
+    ax = torch.empty((1, 64, 64), dtype=torch.float32, device="cuda")
+    aty = torch.empty((1, 500, 432), dtype=torch.float32, device="cuda")
+    f2p.enqueue(dev(x), ax, 0, 1)
+    f2p.enqueue_adjoint(dev(y), aty, 0, 1)
+    lhs = float((host(ax).astype(np.float64) * y).sum())
+    rhs = float((x.astype(np.float64) * host(aty)).sum())
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
