@@ -299,6 +299,10 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     par_copy = torch.randn((B, Pp, Dp), dtype=torch.float32, device=dev)
     t_filt = timed(torch, stream, lambda: filt.enqueue(par_copy, B, stream), reps)
     t_bp = timed(torch, stream, lambda: bp.enqueue(par_buf, img[:B], B, stream), reps)
+    dfx_b = rg.Defects(g, p, max_batch=B)
+    ws_b = torch.empty(dfx_b.workspace_bytes(B), dtype=torch.uint8, device=dev)
+    raw_b = raw[:B].clone()
+    t_def = timed(torch, stream, lambda: dfx_b.enqueue(raw_b, B, ws_b, stream=stream), reps)
     fs, ps = Pf * Df, Pp * Dp
     att_bytes = B * fs * (2 + 4) + L * fs * 4
     f2p_bytes = B * (fs * 4 + ps * 4) + L * ps * 4 * 12
@@ -326,6 +330,7 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
         "filter": {"ms": t_filt, "gbs": filt_bytes / (t_filt / 1e3) / 1e9,
                    "frac_hbm": filt_bytes / (t_filt / 1e3) / 1e9 / hbm},
         "backprojection": {"ms": t_bp},
+        "defects_detect_repair": {"ms": t_def, "gbs": B * fs * 2 * 3 / (t_def / 1e3) / 1e9},
         "hbm_peak_gbs": hbm, "batch": B,
     }
 

@@ -231,6 +231,9 @@ struct risa_gb_backprojection {
       c.mask_value = (float)p.masking_value;
       c.interp = p.interp;
       c.scale = (float)((double)g.Dp / (double)g.N);
+      // t' = t + shift; the texture variant truncates t + Dp/2
+      const double shift = p.quirks == RISA_GB_QUIRKS_RISA ? (double)(int)(g.Dp * 0.5) : g.Dp * 0.5 - 0.5;
+      c.trunc_offset = (float)(g.Dp * 0.5 - shift);
       return c;
    }
 };
@@ -601,8 +604,8 @@ risa_gb_status risa_gb_filter_create(const risa_gb_geometry* gi, const risa_gb_p
    RG_TRY(import_geometry(gi, &h->g, false, true, false));
    RG_TRY(import_params(pi, &h->p));
    RG_TRY(design_filter(h->g, h->p, &h->len, &h->h_host));
-   std::vector<float> tw(h->len);  // interleaved (re, im) of exp(-2 pi i k / len), k < len/2
-   for (int k = 0; k < h->len / 2; ++k) {
+   std::vector<float> tw(2 * (size_t)h->len);  // interleaved (re, im) of exp(-2 pi i k / len), k < len
+   for (int k = 0; k < h->len; ++k) {
       const double ang = -2.0 * 3.14159265358979323846 * (double)k / (double)h->len;
       tw[2 * k] = (float)std::cos(ang);
       tw[2 * k + 1] = (float)std::sin(ang);

@@ -18,17 +18,16 @@ namespace risa_gb {
 
 namespace {
 
-struct Variant {
-   int tx, ty, ppt, achunk;
+// Linear interpolation variants: slices per CTA (S) and angles per chunk of
+// the pair kernel, plus the plain tile kernel. The nearest-neighbour modes
+// always use the plain tile kernel.
+struct PairVariant {
+   int slices, achunk;
    const char* name;
 };
-
-// Tile (tx x ty pixels), pixels per thread along y, angles per chunk.
-constexpr Variant kVariants[] = {
-    {32, 32, 4, 32, "t32x32_p4_a32"},
-    {32, 16, 2, 32, "t32x16_p2_a32"},
-    {32, 32, 4, 16, "t32x32_p4_a16"},
-    {32, 64, 8, 16, "t32x64_p8_a16"},
+constexpr PairVariant kVariants[] = {
+    {2, 32, "pairs_s2_a32"}, {1, 32, "pairs_s1_a32"}, {4, 16, "pairs_s4_a16"},
+    {2, 16, "pairs_s2_a16"}, {4, 32, "pairs_s4_a32"}, {0, 32, "tile32_p4_a32"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -120,10 +119,11 @@ __global__ void __launch_bounds__(TX*(TY / PPT)) bp_tile(const float* __restrict
                k = min(max(k, 0), wlen - 1);
                acc[r] += w[k];
             } else {
-               // truncation toward zero of the global coordinate (texture variant)
-               int k = __float2int_rd(t);
+               // truncation toward zero of t + Dp/2 (texture variant, Backprojection.cu:294)
+               const float tt = t + cfg.trunc_offset;
+               int k = __float2int_rd(tt);
                const int kg = k + s_w0[ai];
-               if (kg == -1 && t != (float)k) k += 1;
+               if (kg == -1 && tt != (float)k) k += 1;
                k = min(max(k, 0), wlen - 1);
                acc[r] += w[k];
             }
@@ -143,6 +143,160 @@ __global__ void __launch_bounds__(TX*(TY / PPT)) bp_tile(const float* __restrict
          out[(size_t)y * N + x] = v;
       }
    }
+}
+
+// ---- linear interpolation, the hot kernel ---------------------------------------
+// A 32x32-pixel tile per CTA, 8 warps; each warp covers 8x4-pixel footprints
+// (so the bins one warp reads for an angle stay within ~16 consecutive
+// window entries, about two shared-memory wavefronts per 64-bit load) and
+// each thread 4 pixels spaced 8 rows apart. S slices of one geometry share a
+// CTA: the ray coordinate, bin index and weight of a pixel are computed once
+// and applied to every slice.
+//
+// The window of an angle holds, for bin k, the pair (midpoint, difference) =
+// ((q[k] + q[k+1]) / 2, q[k+1] - q[k]), so the linearly interpolated value at
+// t = k + 1/2 + f (|f| <= 1/2) is mid + f * diff: one 64-bit shared load,
+// one add and one multiply-add per update. The bin index comes from the
+// round-to-nearest of t - 1/2 via the 1.5 * 2^23 magic constant, without
+// float/int conversion instructions.
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr size_t kMaxPairsSmem = 160 * 1024;
+constexpr int kMagicBits = 0x4B400000;
+
+template <int S>
+__global__ void __launch_bounds__(256) bp_linear_pairs(const float* __restrict__ sino,
+                                                       float* __restrict__ img, BPCfg cfg, int wlen,
+                                                       int ACH, int batch) {
+   constexpr int T = 32, NT = 256;
+   extern __shared__ float2 wsm[];                          // [S][ACH][wlen]
+   float* s_a = reinterpret_cast<float*>(wsm + S * ACH * wlen);
+   float* s_b = s_a + ACH;
+   float* s_rel = s_b + ACH;
+   int* s_w0 = reinterpret_cast<int*>(s_rel + ACH);
+
+   const int N = cfg.N, Dp = cfg.Dp, Pp = cfg.Pp;
+   const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
+   const int s0 = blockIdx.z * S;
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int xo = (warp & 3) * 8 + (lane & 7);
+   const int yo = (warp >> 2) * 4 + (lane >> 3);
+   const float c = 0.5f * (float)(N - 1);
+   const float lim = (float)N * (float)N * 0.25f;
+
+   if (cfg.masking) {
+      const float nx = fminf(fmaxf(c, (float)x0), (float)(x0 + T - 1)) - c;
+      const float ny = fminf(fmaxf(c, (float)y0), (float)(y0 + T - 1)) - c;
+      if (nx * nx + ny * ny > lim) {
+         for (int si = 0; si < S; ++si) {
+            if (s0 + si >= batch) break;
+            float* out = img + (size_t)(s0 + si) * N * N;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+               const int x = x0 + xo, y = y0 + yo + 8 * r;
+               if (x < N && y < N) out[(size_t)y * N + x] = cfg.mask_value;
+            }
+         }
+         return;
+      }
+   }
+
+   float acc[S][4];
+#pragma unroll
+   for (int si = 0; si < S; ++si)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[si][r] = 0.f;
+
+   const unsigned wmax = (unsigned)(wlen - 1);
+   for (int c0 = 0; c0 < Pp; c0 += ACH) {
+      const int na = min(ACH, Pp - c0);
+      if (threadIdx.x < na) {
+         const int ang = c0 + threadIdx.x;
+         const float a = __ldg(cfg.a + ang), b = __ldg(cfg.b + ang);
+         const double base = __ldg(cfg.t0 + ang) + (double)x0 * __ldg(cfg.ad + ang) +
+                             (double)y0 * __ldg(cfg.bd + ang);
+         const double tmin = base + (double)fminf(0.f, (float)(T - 1) * a) +
+                             (double)fminf(0.f, (float)(T - 1) * b);
+         const int w0 = (int)floor(tmin) - 2;
+         s_a[threadIdx.x] = a;
+         s_b[threadIdx.x] = b;
+         s_rel[threadIdx.x] = (float)(base - (double)w0 - 0.5);
+         s_w0[threadIdx.x] = w0;
+      }
+      __syncthreads();
+      const int per_slice = na * wlen;
+      for (int i = threadIdx.x; i < S * per_slice; i += NT) {
+         const int si = i / per_slice, rem = i - si * per_slice;
+         const int ai = rem / wlen, m = rem - ai * wlen;
+         const int k = s_w0[ai] + m;
+         float q0 = 0.f, q1 = 0.f;
+         if (s0 + si < batch) {
+            const float* row = sino + ((size_t)(s0 + si) * Pp + c0 + ai) * Dp;
+            if (k >= 0 && k < Dp) q0 = __ldg(row + k);
+            if (k + 1 >= 0 && k + 1 < Dp) q1 = __ldg(row + k + 1);
+         }
+         wsm[(si * ACH + ai) * wlen + m] = make_float2(0.5f * (q0 + q1), q1 - q0);
+      }
+      __syncthreads();
+#pragma unroll 2
+      for (int ai = 0; ai < na; ++ai) {
+         const float a = s_a[ai], b = s_b[ai];
+         float tm = s_rel[ai] + (float)xo * a + (float)yo * b;
+         const float step = 8.f * b;
+#pragma unroll
+         for (int r = 0; r < 4; ++r) {
+            const float v = tm + kMagic;
+            const float f = tm - (v - kMagic);
+            const unsigned k = min((unsigned)(__float_as_int(v) - kMagicBits), wmax);
+#pragma unroll
+            for (int si = 0; si < S; ++si) {
+               const float2 p = wsm[(si * ACH + ai) * wlen + k];
+               acc[si][r] = fmaf(f, p.y, acc[si][r] + p.x);
+            }
+            tm += step;
+         }
+      }
+      __syncthreads();
+   }
+#pragma unroll
+   for (int si = 0; si < S; ++si) {
+      if (s0 + si >= batch) break;
+      float* out = img + (size_t)(s0 + si) * N * N;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+         const int x = x0 + xo, y = y0 + yo + 8 * r;
+         if (x < N && y < N) {
+            float v = acc[si][r] * cfg.norm;
+            if (cfg.masking) {
+               const float dx = (float)x - c, dy = (float)y - c;
+               if (dx * dx + dy * dy > lim) v = cfg.mask_value;
+            }
+            out[(size_t)y * N + x] = v;
+         }
+      }
+   }
+}
+
+// Shared memory of one CTA: S windows of ach angles plus the per-angle scalars.
+inline size_t pairs_smem(int S, int ach, int wlen) {
+   return sizeof(float2) * (size_t)S * ach * wlen + sizeof(float) * 4 * ach;
+}
+
+template <int S>
+cudaError_t launch_pairs(const float* sino, float* img, int batch, const BPCfg& cfg, int ach,
+                         cudaStream_t st) {
+   const int wlen = window_len(cfg.scale, 32, 32);
+   // wide windows (many bins per pixel) get shorter angle chunks
+   while (ach > 4 && pairs_smem(S, ach, wlen) > kMaxPairsSmem) ach /= 2;
+   const size_t smem = pairs_smem(S, ach, wlen);
+   if (smem > kMaxPairsSmem) return cudaErrorInvalidConfiguration;
+   auto kern = bp_linear_pairs<S>;
+   if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+   }
+   dim3 grid((cfg.N + 31) / 32, (cfg.N + 31) / 32, (batch + S - 1) / S);
+   kern<<<grid, 256, smem, st>>>(sino, img, cfg, wlen, ach, batch);
+   return cudaGetLastError();
 }
 
 template <int TX, int TY, int PPT, int ACH, int INTERP>
@@ -227,11 +381,14 @@ const char* bp_variant_name(int v) {
 cudaError_t launch_backprojection(const float* sino, float* img, int batch, const BPCfg& cfg,
                                   int variant, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
-   switch (variant) {
-      case 1: return launch_interp<32, 16, 2, 32>(sino, img, batch, cfg, st);
-      case 2: return launch_interp<32, 32, 4, 16>(sino, img, batch, cfg, st);
-      case 3: return launch_interp<32, 64, 8, 16>(sino, img, batch, cfg, st);
-      default: return launch_interp<32, 32, 4, 32>(sino, img, batch, cfg, st);
+   if (cfg.interp != RISA_GB_INTERP_LINEAR || variant < 0 || variant >= kNumVariants ||
+       kVariants[variant].slices == 0)
+      return launch_interp<32, 32, 4, 32>(sino, img, batch, cfg, st);
+   const PairVariant& v = kVariants[variant];
+   switch (v.slices) {
+      case 1: return launch_pairs<1>(sino, img, batch, cfg, v.achunk, st);
+      case 2: return launch_pairs<2>(sino, img, batch, cfg, v.achunk, st);
+      default: return launch_pairs<4>(sino, img, batch, cfg, v.achunk, st);
    }
 }
 

@@ -15,7 +15,7 @@ namespace risa_gb {
 
 namespace {
 constexpr int kThreads = 256;
-constexpr int kFramesPerThread = 4;
+constexpr int kFramesPerThread = 8;
 
 __device__ __forceinline__ float bilinear(const float* __restrict__ f, uint32_t pk, float u, float v,
                                           int Pf, int Df) {

@@ -4,39 +4,102 @@
 // the applyFilter kernel (:231-241) and a C2R in place -- three launches and a
 // complex scratch buffer round trip through global memory per frame. Here one
 // CTA owns whole rows: two real rows are packed as one complex row
-// (z = a + i*b), zero padded to the FFT length, transformed forward with a
-// radix-2 Stockham FFT in shared memory, multiplied by the real, even filter
-// response (which keeps both rows' spectra Hermitian, so no unpacking is
-// needed), transformed back, and the real and imaginary parts are stored as
-// the two filtered rows. Twiddles come from an FP64-built table.
+// (z = a + i*b), zero padded to the FFT length, transformed with a
+// mixed-radix (8, then 4 or 2) Stockham FFT whose butterflies run in
+// registers and whose passes exchange data through shared memory, multiplied
+// by the real, even filter response (which keeps both rows' spectra
+// Hermitian, so no unpacking is needed) and transformed back. The inverse
+// reuses the forward transform through conj(FFT(conj(.))). Twiddles come from
+// an FP64-built table; global memory is touched once per row in each
+// direction.
 #include "kernels.h"
 
 namespace risa_gb {
 
 namespace {
 constexpr int kThreads = 256;
+constexpr float kSqrtHalf = 0.70710678118654752f;
 
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // * (-i)
 
-// One radix-2 Stockham pass: out[expand(j)] = butterfly(in[j], in[j + len/2]).
-template <bool INVERSE>
-__device__ __forceinline__ void stockham_pass(const float2* __restrict__ in, float2* __restrict__ out,
-                                              const float2* __restrict__ tw, int len, int ns,
-                                              int lt, int tpp) {
-   const int half = len >> 1;
-   const int tstride = len / (2 * ns);
-   for (int j = lt; j < half; j += tpp) {
+__device__ __forceinline__ void dft2(float2* v) {
+   const float2 t = v[0];
+   v[0] = cadd(t, v[1]);
+   v[1] = csub(t, v[1]);
+}
+
+__device__ __forceinline__ void dft4(float2& x0, float2& x1, float2& x2, float2& x3) {
+   const float2 t0 = cadd(x0, x2), t1 = csub(x0, x2);
+   const float2 t2 = cadd(x1, x3), t3 = mul_mi(csub(x1, x3));
+   x0 = cadd(t0, t2);
+   x2 = csub(t0, t2);
+   x1 = cadd(t1, t3);
+   x3 = csub(t1, t3);
+}
+
+__device__ __forceinline__ void dft8(float2* v) {
+   // radix-2 decimation in time over two 4-point transforms
+   float2 a0 = v[0], a1 = v[2], a2 = v[4], a3 = v[6];
+   float2 b0 = v[1], b1 = v[3], b2 = v[5], b3 = v[7];
+   dft4(a0, a1, a2, a3);
+   dft4(b0, b1, b2, b3);
+   b1 = make_float2(kSqrtHalf * (b1.x + b1.y), kSqrtHalf * (b1.y - b1.x));    // * W8^1
+   b2 = mul_mi(b2);                                                           // * W8^2
+   b3 = make_float2(kSqrtHalf * (b3.y - b3.x), -kSqrtHalf * (b3.x + b3.y));   // * W8^3
+   v[0] = cadd(a0, b0); v[4] = csub(a0, b0);
+   v[1] = cadd(a1, b1); v[5] = csub(a1, b1);
+   v[2] = cadd(a2, b2); v[6] = csub(a2, b2);
+   v[3] = cadd(a3, b3); v[7] = csub(a3, b3);
+}
+
+// One Stockham pass of radix R: combines R sub-transforms of length ns.
+template <int R>
+__device__ __forceinline__ void pass(const float2* __restrict__ in, float2* __restrict__ out,
+                                     const float2* __restrict__ tw, int len, int ns, int lt, int tpp) {
+   const int stride = len / R;
+   const int tstep = len / (R * ns);
+   for (int j = lt; j < stride; j += tpp) {
       const int k = j & (ns - 1);
-      float2 w = __ldg(tw + k * tstride);
-      if (INVERSE) w.y = -w.y;
-      const float2 v0 = in[j];
-      const float2 v1 = cmul(in[j + half], w);
-      const int d = ((j - k) << 1) + k;
-      out[d] = make_float2(v0.x + v1.x, v0.y + v1.y);
-      out[d + ns] = make_float2(v0.x - v1.x, v0.y - v1.y);
+      float2 v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = in[j + r * stride];
+      if (ns > 1) {
+#pragma unroll
+         for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(tw + r * k * tstep));
+      }
+      if (R == 8) dft8(v);
+      else if (R == 4) dft4(v[0], v[1], v[2], v[3]);
+      else dft2(v);
+      const int d = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) out[d + r * ns] = v[r];
    }
+}
+
+// Full forward transform; returns the buffer holding the result.
+__device__ float2* fft(float2* a, float2* b, const float2* tw, int len, int lt, int tpp) {
+   int ns = 1;
+   while (ns < len) {
+      const int rest = len / ns;
+      if (rest % 8 == 0 && rest != 16) {  // 16 = 4 * 4 splits better than 8 * 2
+         pass<8>(a, b, tw, len, ns, lt, tpp);
+         ns *= 8;
+      } else if (rest % 4 == 0) {
+         pass<4>(a, b, tw, len, ns, lt, tpp);
+         ns *= 4;
+      } else {
+         pass<2>(a, b, tw, len, ns, lt, tpp);
+         ns *= 2;
+      }
+      __syncthreads();
+      float2* t = a; a = b; b = t;
+   }
+   return a;
 }
 
 // grid.x: groups of row pairs. Dynamic smem: pairs_per_block * 2 * len float2.
@@ -60,27 +123,19 @@ __global__ void __launch_bounds__(kThreads) filter_rows(float* __restrict__ sino
       x0[n] = make_float2(a, b);
    }
    __syncthreads();
-   float2* src = x0;
-   float2* dst = x1;
-   for (int ns = 1; ns < len; ns <<= 1) {
-      stockham_pass<false>(src, dst, cfg.twiddle, len, ns, lt, tpp);
-      __syncthreads();
-      float2* t = src; src = dst; dst = t;
-   }
+   float2* spec = fft(x0, x1, cfg.twiddle, len, lt, tpp);
+   float2* other = spec == x0 ? x1 : x0;
+   // filter, conjugate for the inverse: ifft(Z) = conj(fft(conj(Z))) / len (the 1/len is in h)
    for (int k = lt; k < len; k += tpp) {
       const float h = __ldg(cfg.h + (k <= (len >> 1) ? k : len - k));
-      src[k].x *= h;
-      src[k].y *= h;
+      const float2 z = spec[k];
+      spec[k] = make_float2(z.x * h, -z.y * h);
    }
    __syncthreads();
-   for (int ns = 1; ns < len; ns <<= 1) {
-      stockham_pass<true>(src, dst, cfg.twiddle, len, ns, lt, tpp);
-      __syncthreads();
-      float2* t = src; src = dst; dst = t;
-   }
+   float2* res = fft(spec, other, cfg.twiddle, len, lt, tpp);
    for (int n = lt; n < Dp; n += tpp) {
-      if (has_a) row_a[n] = src[n].x;
-      if (has_b) row_b[n] = src[n].y;
+      if (has_a) row_a[n] = res[n].x;
+      if (has_b) row_b[n] = -res[n].y;
    }
 }
 }  // namespace
@@ -88,7 +143,7 @@ __global__ void __launch_bounds__(kThreads) filter_rows(float* __restrict__ sino
 cudaError_t launch_filter(float* sino, int batch, const FilterCfg& cfg, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
    const int total_rows = batch * cfg.rows;
-   const int tpp = cfg.len / 2 < kThreads ? cfg.len / 2 : kThreads;
+   const int tpp = cfg.len / 8 < kThreads ? cfg.len / 8 : kThreads;
    const int ppb = kThreads / tpp;
    const int pairs = (total_rows + 1) / 2;
    const size_t smem = sizeof(float2) * 2 * (size_t)cfg.len * ppb;

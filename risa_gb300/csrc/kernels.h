@@ -91,7 +91,7 @@ cudaError_t launch_fan2para_adjoint(const float* par, float* fan, int batch, con
 // ---------------------------------------------------------------- filter
 struct FilterCfg {
    int rows, Dp, len;
-   const float2* twiddle;  // [len/2] exp(-2 pi i k / len)
+   const float2* twiddle;  // [len] exp(-2 pi i k / len)
    const float* h;         // [len/2 + 1]
 };
 cudaError_t launch_filter(float* sino, int batch, const FilterCfg& cfg, cudaStream_t st);
@@ -109,6 +109,7 @@ struct BPCfg {
    float mask_value;
    int interp;          // RISA_GB_INTERP_*
    float scale;         // Dp / N (bins per pixel)
+   float trunc_offset;  // texture variant truncates t' + trunc_offset (= t + Dp/2)
 };
 int bp_variant_count();
 const char* bp_variant_name(int v);

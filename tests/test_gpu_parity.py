@@ -226,9 +226,11 @@ def test_masking_normalisation():
 
 # ------------------------------------------------------------------------------ whole chain
 def _fbp_case(quirk, defects, masking, L=1, frames=3):
+    # the reference's unpadded filter needs a power-of-two ray count
+    dp = 128 if quirk == rg.QUIRKS_RISA else 96
     d = dict(SMALL, n_planes=L, source_diameter=[430.0] * L, delta_x=[0.0] * L,
              delta_z=[1417.0 + 13 * k for k in range(L)], source_angle=[360.0] * L,
-             n_par_proj=96, n_par_det=96, n_pixels=96)
+             n_par_proj=96, n_par_det=dp, n_pixels=96)
     sc = phantom.make_scan(frames, L, 500, 432, 215.0, 240.0, seed=11, defect_fraction=0.01 if defects else 0,
                            distinct=frames)
     ftype = "sheppLogan"
