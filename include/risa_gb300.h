@@ -107,6 +107,10 @@ typedef struct risa_gb_params {
    double masking_value;     /* maskingValue */
    int32_t normalize;        /* min-max normalisation before masking */
    int32_t repair_reference; /* repair defects in reference frames at init */
+   int32_t module_major;     /* raw frames arrive module-major, [module][proj][det in module],
+                                as the reference's loader reads them; the reordering of its
+                                Reordering stage (Reordering.cu:180-204) is then fused into
+                                the defect and attenuation kernels (n_modules from geometry) */
 } risa_gb_params;
 
 /* Fill defaults (ramp, cutoff 1, auto pad, linear, NONE quirks, thresholds
@@ -122,6 +126,19 @@ const char* risa_gb_version(void);
  * parsed by this library (key = value; lists in [ ]). Replaces the
  * ConfigReader + readConfig pair of every stage (ConfigReader.h:62-86). */
 risa_gb_status risa_gb_config_load(const char* path, risa_gb_geometry* g, risa_gb_params* p);
+/* Any single setting as text (strings unquoted, arrays as comma-separated
+ * values), for the keys a stage reads beyond geometry and params
+ * (paths, file names, pool sizes, frame counts). RISA_GB_ECONFIG if absent. */
+risa_gb_status risa_gb_config_lookup(const char* path, const char* key, char* value,
+                                     size_t value_len);
+
+/* ---------------------------------------------------------------------------
+ * Reordering (Reordering.cu:118-204): module-major raw frames
+ * [n_modules][n_fan_proj][n_fan_det/n_modules] -> detector-major
+ * [n_fan_proj][n_fan_det]; any module count that divides n_fan_det (the
+ * reference hard-codes 27 modules of 16 detectors). Stateless. */
+risa_gb_status risa_gb_reorder_enqueue(const uint16_t* in, uint16_t* out, int n_modules,
+                                       int n_fan_proj, int n_fan_det, int batch, void* stream);
 
 /* ---------------------------------------------------------------------------
  * DetectorInterpolation (DetectorInterpolation.cu:105-140; algorithm

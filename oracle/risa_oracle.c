@@ -109,7 +109,9 @@ static void interpolate_risa(uint16_t* data, const int* flags, unsigned D, unsig
    }
 }
 
-/* Physically correct variant: circular runs, FP64 weights, rounding to nearest. */
+/* Physically correct variant: circular runs (each run between its two good
+ * neighbours), FP32 weights and combination as in RISA mode, rounding to the
+ * nearest uint16 instead of truncating. */
 static void interpolate_none(uint16_t* data, const int* flags, unsigned D, unsigned P) {
    unsigned start = D;
    for (unsigned d = 0; d < D; ++d)
@@ -124,11 +126,12 @@ static void interpolate_none(uint16_t* data, const int* flags, unsigned D, unsig
       const unsigned left = (start + k - 1u) % D, right = (start + k + len) % D;
       for (unsigned m = 0; m < len; ++m) {
          const unsigned col = (start + k + m) % D;
-         const double w1 = (double)(m + 1u) / (double)(len + 1u);
-         const double w0 = 1.0 - w1;
+         const float w1 = (float)(m + 1u) / (float)(len + 1u);
+         const float w0 = 1.0f - w1;
          for (unsigned p = 0; p < P; ++p) {
-            const double v = w0 * (double)data[left + p * D] + w1 * (double)data[right + p * D];
-            data[col + p * D] = (uint16_t)floor(v + 0.5);
+            const float a = w0 * (float)data[left + p * D];
+            const float b = w1 * (float)data[right + p * D];
+            data[col + p * D] = (uint16_t)floorf((a + b) + 0.5f);
          }
       }
       k += len;

@@ -58,7 +58,7 @@ class Params(ctypes.Structure):
         ("xa", ctypes.c_uint32), ("xb", ctypes.c_uint32), ("xc", ctypes.c_uint32),
         ("xd", ctypes.c_uint32), ("xe", ctypes.c_uint32), ("xf", ctypes.c_uint32),
         ("masking", ctypes.c_int32), ("masking_value", ctypes.c_double), ("normalize", ctypes.c_int32),
-        ("repair_reference", ctypes.c_int32),
+        ("repair_reference", ctypes.c_int32), ("module_major", ctypes.c_int32),
     ]
 
 
@@ -71,6 +71,8 @@ SIGNATURES = {
     "risa_gb_last_error": (ctypes.c_char_p, []),
     "risa_gb_version": (ctypes.c_char_p, []),
     "risa_gb_config_load": (_i, [ctypes.c_char_p, _vp, _vp]),
+    "risa_gb_config_lookup": (_i, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _sz]),
+    "risa_gb_reorder_enqueue": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
     "risa_gb_defects_create": (_i, [_vp, _vp, _i, _pp]),
     "risa_gb_defects_workspace_bytes": (_sz, [_vp, _i]),
     "risa_gb_defects_enqueue": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
@@ -183,7 +185,8 @@ def make_geometry(n_planes=1, n_fan_det=432, n_fan_proj=500, n_par_proj=256, n_p
 def make_params(quirks=QUIRKS_NONE, filter_type="ramp", cutoff=1.0, pad=0, interp=INTERP_LINEAR,
                 defects=False, thresh_min=0.67, thresh_max=1.5, relevant_mask=False,
                 lower_lim_offset=0.0, upper_lim_offset=0.0, fix_points=(0, 0, 0, 0, 0, 0),
-                masking=False, masking_value=0.0, normalize=False, repair_reference=True) -> Params:
+                masking=False, masking_value=0.0, normalize=False, repair_reference=True,
+                module_major=False) -> Params:
     p = Params()
     lib().risa_gb_params_init(ctypes.byref(p))
     p.quirks = quirks
@@ -195,6 +198,7 @@ def make_params(quirks=QUIRKS_NONE, filter_type="ramp", cutoff=1.0, pad=0, inter
     p.xa, p.xb, p.xc, p.xd, p.xe, p.xf = (int(v) for v in fix_points)
     p.masking, p.masking_value, p.normalize = int(masking), masking_value, int(normalize)
     p.repair_reference = int(repair_reference)
+    p.module_major = int(module_major)
     return p
 
 
@@ -202,6 +206,27 @@ def load_config(path: str):
     g, p = Geometry(), Params()
     _check(lib().risa_gb_config_load(path.encode(), ctypes.byref(g), ctypes.byref(p)), "config_load")
     return g, p
+
+
+def config_lookup(path: str, key: str) -> str:
+    """One setting of a config file as text (arrays comma-separated)."""
+    buf = ctypes.create_string_buffer(4096)
+    _check(lib().risa_gb_config_lookup(path.encode(), key.encode(), buf, len(buf)), "config_lookup")
+    return buf.value.decode()
+
+
+def reorder(inp, out, n_modules: int, n_fan_proj: int, n_fan_det: int, batch: int, stream=None):
+    """Module-major -> detector-major raw frames on the device (the Reordering stage)."""
+    _check(lib().risa_gb_reorder_enqueue(ptr(inp), ptr(out), n_modules, n_fan_proj, n_fan_det, batch,
+                                         stream_ptr(stream)), "reorder_enqueue")
+
+
+def to_module_major(frames, n_modules: int):
+    """Host helper: detector-major [..., P, D] -> module-major [..., modules, P, D/modules]."""
+    import numpy as np
+    *lead, P, D = frames.shape
+    w = D // n_modules
+    return np.ascontiguousarray(frames.reshape(*lead, P, n_modules, w).swapaxes(-3, -2))
 
 
 def geometry_dict(g: Geometry) -> dict:

@@ -72,7 +72,29 @@ def build(verbose: bool = False) -> str:
         if res.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
         os.replace(tmp, LIB)
+    _build_pipeline()
     return LIB
+
+
+PIPELINE = os.path.join(BUILD, "risa_gb_pipeline")
+
+
+def _build_pipeline():
+    """The configuration-driven pipeline example (C++ stages over the C ABI)."""
+    src = os.path.join(PKG, "cpp", "examples", "risa_gb_pipeline.cpp")
+    deps = [src, LIB] + glob.glob(os.path.join(PKG, "cpp", "*", "*.h"))
+    if os.path.exists(PIPELINE) and all(os.path.getmtime(d) <= os.path.getmtime(PIPELINE) for d in deps):
+        return PIPELINE
+    tmp = PIPELINE + f".tmp{os.getpid()}"
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    cmd = ["g++", "-std=c++17", "-O2", "-pthread", "-I", INCLUDE, "-I", os.path.join(cuda, "include"), src,
+           "-o", tmp, "-L", BUILD, "-lrisa_gb300", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+           "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"pipeline build failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, PIPELINE)
+    return PIPELINE
 
 
 if __name__ == "__main__":

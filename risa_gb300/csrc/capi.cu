@@ -77,6 +77,12 @@ struct DevBuf {
 
 inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
 
+risa_gb_status check_layout(const Geometry& g, const Params& p) {
+   if (p.module_major && (g.modules < 1 || g.Df % g.modules != 0))
+      return fail(RISA_GB_EINVAL, "module-major frames need n_modules >= 1 dividing n_fan_det");
+   return RISA_GB_OK;
+}
+
 risa_gb_status check_plane(const Geometry& g, int plane) {
    if (plane != RISA_GB_PLANES_INTERLEAVED && (plane < 0 || plane >= g.L))
       return fail(RISA_GB_EINVAL, "plane out of range");
@@ -146,6 +152,7 @@ risa_gb_status import_params(const risa_gb_params* in, Params* p) {
    p->masking_value = in->masking_value;
    p->normalize = in->normalize;
    p->repair_reference = in->repair_reference;
+   p->module_major = in->module_major;
    if (p->quirks != RISA_GB_QUIRKS_NONE && p->quirks != RISA_GB_QUIRKS_RISA)
       return fail(RISA_GB_EINVAL, "unknown quirks mode");
    if (p->filter_type < 0 || p->filter_type > 4) return fail(RISA_GB_EINVAL, "unknown filter type");
@@ -179,6 +186,7 @@ struct risa_gb_attenuation {
       c.mask = p.relevant_mask ? mask.as<uint32_t>() : nullptr;
       c.wpr = wpr;
       c.quirk = p.quirks;
+      c.modules = p.module_major ? g.modules : 0;
       return c;
    }
 };
@@ -306,6 +314,19 @@ risa_gb_status risa_gb_config_load(const char* path, risa_gb_geometry* g, risa_g
    return load_config(path, g, p);
 }
 
+risa_gb_status risa_gb_config_lookup(const char* path, const char* key, char* value, size_t value_len) {
+   return lookup_config(path, key, value, value_len);
+}
+
+risa_gb_status risa_gb_reorder_enqueue(const uint16_t* in, uint16_t* out, int n_modules, int n_fan_proj,
+                                       int n_fan_det, int batch, void* stream) {
+   if (!in || !out || in == out) return fail(RISA_GB_EINVAL, "reorder needs distinct input and output");
+   if (n_modules < 1 || n_fan_det % n_modules || n_fan_proj < 1 || batch < 0)
+      return fail(RISA_GB_EINVAL, "reorder: n_modules must divide n_fan_det");
+   RG_CUDA(launch_reorder(in, out, n_modules, n_fan_proj, n_fan_det, batch, S(stream)));
+   return RISA_GB_OK;
+}
+
 // ---------------------------------------------------------------------------- defects
 risa_gb_status risa_gb_defects_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
                                       int max_batch, risa_gb_defects** out) {
@@ -315,6 +336,7 @@ risa_gb_status risa_gb_defects_create(const risa_gb_geometry* gi, const risa_gb_
    if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
    RG_TRY(import_geometry(gi, &h->g, true, false, false));
    RG_TRY(import_params(pi, &h->p));
+   RG_TRY(check_layout(h->g, h->p));
    if (max_batch < 1) return fail(RISA_GB_EINVAL, "max_batch must be >= 1");
    h->max_batch = max_batch;
    h->cfg.P = h->g.Pf;
@@ -323,6 +345,7 @@ risa_gb_status risa_gb_defects_create(const risa_gb_geometry* gi, const risa_gb_
    h->cfg.thresh_max = h->p.thresh_max;
    h->cfg.quirk = h->p.quirks;
    h->cfg.max_runs = h->g.Df / 2 + 2;
+   h->cfg.modules = h->p.module_major ? h->g.modules : 0;
    RG_CUDA(upload_defect_filter(0));
    RG_CUDA(cudaStreamSynchronize(0));
    *out = h.release();
@@ -360,6 +383,7 @@ risa_gb_status risa_gb_attenuation_create(const risa_gb_geometry* gi, const risa
    if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
    RG_TRY(import_geometry(gi, &h->g, true, false, false));
    RG_TRY(import_params(pi, &h->p));
+   RG_TRY(check_layout(h->g, h->p));
    if (!ref_frames || n_ref < 1) return fail(RISA_GB_EINVAL, "at least one reference frame is required");
    const Geometry& g = h->g;
    const size_t fs = (size_t)g.Pf * g.Df;
@@ -372,6 +396,7 @@ risa_gb_status risa_gb_attenuation_create(const risa_gb_geometry* gi, const risa
       risa_gb_defects* dh = nullptr;
       RG_TRY(risa_gb_defects_create(gi, pi, (int)nref_frames, &dh));
       std::unique_ptr<risa_gb_defects, risa_gb_status (*)(risa_gb_defects*)> guard(dh, risa_gb_defects_destroy);
+      dh->cfg.modules = 0;  // reference frames are handed over detector-major
       DevBuf ws;
       RG_TRY(ws.alloc(risa_gb_defects_workspace_bytes(dh, (int)nref_frames)));
       RG_TRY(risa_gb_defects_enqueue(dh, d_ref.as<uint16_t>(), (int)nref_frames, nullptr, ws.p, nullptr));

@@ -9,6 +9,7 @@
 
 #include <cctype>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <map>
 #include <sstream>
@@ -160,18 +161,59 @@ struct Parser {
 };
 }  // namespace
 
-risa_gb_status load_config(const char* path, risa_gb_geometry* g, risa_gb_params* p) {
-   if (!path || !g || !p) return fail(RISA_GB_EINVAL, "config: null argument");
+namespace {
+risa_gb_status parse_file(const char* path, std::map<std::string, Value>* kv) {
    std::ifstream in(path);
    if (!in) return fail(RISA_GB_ECONFIG, std::string("config: cannot open ") + path);
    std::stringstream ss;
    ss << in.rdbuf();
    Parser ps;
    ps.s = ss.str();
-   std::map<std::string, Value> kv;
-   if (!ps.parse(&kv))
+   if (!ps.parse(kv))
       return fail(RISA_GB_ECONFIG, std::string("config: parse error at ") + path + ":" +
                                        std::to_string(ps.line) + " - " + ps.err);
+   return RISA_GB_OK;
+}
+
+std::string to_text(const Value& v) {
+   switch (v.kind) {
+      case Value::kString: return v.str;
+      case Value::kBool: return v.num != 0.0 ? "true" : "false";
+      case Value::kNumber: {
+         if (v.is_int) return std::to_string(v.inum);
+         std::ostringstream os;
+         os.precision(17);
+         os << v.num;
+         return os.str();
+      }
+      case Value::kArray: {
+         std::string out;
+         for (size_t i = 0; i < v.items.size(); ++i) out += (i ? "," : "") + to_text(v.items[i]);
+         return out;
+      }
+      default: return "";
+   }
+}
+}  // namespace
+
+risa_gb_status lookup_config(const char* path, const char* key, char* value, size_t value_len) {
+   if (!path || !key || !value || value_len == 0) return fail(RISA_GB_EINVAL, "config: null argument");
+   std::map<std::string, Value> kv;
+   risa_gb_status st = parse_file(path, &kv);
+   if (st) return st;
+   auto it = kv.find(key);
+   if (it == kv.end()) return fail(RISA_GB_ECONFIG, std::string("config: no setting ") + key);
+   const std::string text = to_text(it->second);
+   if (text.size() + 1 > value_len) return fail(RISA_GB_EINVAL, "config: value buffer too small");
+   std::memcpy(value, text.c_str(), text.size() + 1);
+   return RISA_GB_OK;
+}
+
+risa_gb_status load_config(const char* path, risa_gb_geometry* g, risa_gb_params* p) {
+   if (!path || !g || !p) return fail(RISA_GB_EINVAL, "config: null argument");
+   std::map<std::string, Value> kv;
+   risa_gb_status pst = parse_file(path, &kv);
+   if (pst) return pst;
    risa_gb_geometry_init(g);
    risa_gb_params_init(p);
    auto num = [&](const char* k, double* out) {
@@ -275,6 +317,7 @@ risa_gb_status load_config(const char* path, risa_gb_geometry* g, risa_gb_params
    if (num("gb_relevant_mask", &d)) p->relevant_mask = d != 0.0;
    if (num("gb_masking", &d)) p->masking = d != 0.0;
    if (num("gb_repair_reference", &d)) p->repair_reference = d != 0.0;
+   if (num("gb_module_major", &d)) p->module_major = d != 0.0;
    return RISA_GB_OK;
 }
 

@@ -16,7 +16,7 @@ namespace risa_gb {
 
 namespace {
 constexpr int kThreads = 256;
-constexpr int kRows = 8;        // rows per CTA in the fused-repair path
+constexpr int kRows = 16;       // rows per CTA in the fused-repair path
 constexpr float kClamp = 1e-5f; // the reference's `temp` (Attenuation.cu:144)
 
 __device__ __forceinline__ int frame_plane(int b, int plane, int L) {
@@ -44,7 +44,9 @@ __global__ void __launch_bounds__(kThreads) attenuation_vec8(const uint16_t* __r
    const size_t i8 = ((size_t)blockIdx.x * kThreads + threadIdx.x) * 8;
    if (i8 >= fs) return;
    const int y = (int)(i8 / cfg.D), x = (int)(i8 % cfg.D);
-   const uint4 r = __ldg(reinterpret_cast<const uint4*>(raw + (size_t)b * fs + i8));
+   // 8 consecutive detectors never straddle a module (module width % 8 == 0)
+   const uint4 r = __ldg(reinterpret_cast<const uint4*>(raw + (size_t)b * fs +
+                                                        raw_offset(y, x, cfg.P, cfg.D, cfg.modules)));
    const float4* ld = reinterpret_cast<const float4*>(cfg.logden + (size_t)k * fs + i8);
    const float4* dk = reinterpret_cast<const float4*>(cfg.dark + (size_t)k * cfg.D + x);
    const float4 l0 = __ldg(ld), l1 = __ldg(ld + 1);
@@ -78,29 +80,45 @@ __global__ void __launch_bounds__(kThreads) attenuation_scalar(const uint16_t* _
    const size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x;
    if (i >= fs) return;
    const int y = (int)(i / cfg.D), x = (int)(i % cfg.D);
-   float v = atten_one(__ldg(raw + (size_t)b * fs + i), __ldg(cfg.dark + (size_t)k * cfg.D + x),
+   float v = atten_one(__ldg(raw + (size_t)b * fs + raw_offset(y, x, cfg.P, cfg.D, cfg.modules)),
+                       __ldg(cfg.dark + (size_t)k * cfg.D + x),
                        __ldg(cfg.logden + (size_t)k * fs + i));
    if (!mask_keep(cfg.mask, cfg.wpr, y, x)) v = 0.f;
    out[(size_t)b * fs + i] = v;
 }
 
-// Fused defect repair + attenuation: kRows rows of one frame per CTA.
+// Fused defect repair + attenuation: kRows rows of one frame per CTA. The rows
+// are staged in shared memory (16-byte loads), one thread per row applies the
+// frame's defect runs in list order (so a run that reads a column repaired by
+// an earlier run sees the repaired value, as in the reference's sequential
+// loop), then every thread converts 8 samples at a time.
 __global__ void __launch_bounds__(kThreads) attenuation_repair(const uint16_t* __restrict__ raw,
                                                                float* __restrict__ out,
                                                                AttenuationCfg cfg,
                                                                const int* __restrict__ counts,
                                                                const DefectRun* __restrict__ runs,
                                                                int max_runs) {
-   extern __shared__ uint16_t tile[];  // [kRows][D]
+   extern __shared__ __align__(16) uint16_t tile[];  // [kRows][D]
    const int D = cfg.D;
    const size_t fs = (size_t)cfg.P * D;
    const int b = blockIdx.y;
    const int k = frame_plane(b, cfg.plane, cfg.L);
    const int y0 = blockIdx.x * kRows;
    const int rows = min(kRows, cfg.P - y0);
-   const uint16_t* src = raw + (size_t)b * fs + (size_t)y0 * D;
+   const uint16_t* frame = raw + (size_t)b * fs;
    const int n = rows * D;
-   for (int i = threadIdx.x; i < n; i += kThreads) tile[i] = src[i];
+   const bool vec = (D % 8) == 0 && (cfg.modules <= 0 || ((D / cfg.modules) % 8) == 0);
+   if (vec) {
+      // 8 consecutive detectors are contiguous in either layout
+      for (int i8 = threadIdx.x * 8; i8 < n; i8 += kThreads * 8) {
+         const int y = y0 + i8 / D, x = i8 % D;
+         *reinterpret_cast<uint4*>(tile + i8) =
+             __ldg(reinterpret_cast<const uint4*>(frame + raw_offset(y, x, cfg.P, D, cfg.modules)));
+      }
+   } else {
+      for (int i = threadIdx.x; i < n; i += kThreads)
+         tile[i] = frame[raw_offset(y0 + i / D, i % D, cfg.P, D, cfg.modules)];
+   }
    __syncthreads();
    const int nr = counts[b];
    if (threadIdx.x < rows && nr > 0) {
@@ -108,32 +126,46 @@ __global__ void __launch_bounds__(kThreads) attenuation_repair(const uint16_t* _
       const DefectRun* rl = runs + (size_t)b * max_runs;
       for (int r = 0; r < nr; ++r) {
          const DefectRun run = rl[r];
-         for (int m = 0; m < run.len; ++m) {
-            uint16_t val;
-            if (cfg.quirk == RISA_GB_QUIRKS_RISA) {
-               const float w1 = (float)__ddiv_rn((double)m + 1.0, (double)run.len + 1.0);
-               const float w0 = (float)__dsub_rn(1.0, (double)w1);
-               val = (uint16_t)__float2uint_rz(__fadd_rn(__fmul_rn(w0, (float)row[run.left]),
-                                                         __fmul_rn(w1, (float)row[run.right])));
-            } else {
-               const double w1 = __ddiv_rn((double)(m + 1), (double)(run.len + 1));
-               const double w0 = __dsub_rn(1.0, w1);
-               val = (uint16_t)floor(__dadd_rn(__dmul_rn(w0, (double)row[run.left]),
-                                               __dmul_rn(w1, (double)row[run.right])) + 0.5);
-            }
-            row[(run.start + m) % D] = val;
-         }
+         for (int m = 0; m < run.len; ++m) row[(run.start + m) % D] = repair_value(row, run, m, cfg.quirk);
       }
    }
    __syncthreads();
    const float* ld = cfg.logden + (size_t)k * fs + (size_t)y0 * D;
    const float* dk = cfg.dark + (size_t)k * D;
    float* dst = out + (size_t)b * fs + (size_t)y0 * D;
-   for (int i = threadIdx.x; i < n; i += kThreads) {
-      const int x = i % D;
-      float v = atten_one(tile[i], __ldg(dk + x), __ldg(ld + i));
-      if (!mask_keep(cfg.mask, cfg.wpr, y0 + i / D, x)) v = 0.f;
-      __stcs(dst + i, v);
+   if ((D % 8) == 0) {
+      for (int i8 = threadIdx.x * 8; i8 < n; i8 += kThreads * 8) {
+         const int x = i8 % D, y = y0 + i8 / D;
+         const uint4 r = *reinterpret_cast<const uint4*>(tile + i8);
+         const float4 l0 = __ldg(reinterpret_cast<const float4*>(ld + i8));
+         const float4 l1 = __ldg(reinterpret_cast<const float4*>(ld + i8) + 1);
+         const float4 d0 = __ldg(reinterpret_cast<const float4*>(dk + x));
+         const float4 d1 = __ldg(reinterpret_cast<const float4*>(dk + x) + 1);
+         float v[8];
+         v[0] = atten_one(r.x & 0xFFFFu, d0.x, l0.x);
+         v[1] = atten_one(r.x >> 16, d0.y, l0.y);
+         v[2] = atten_one(r.y & 0xFFFFu, d0.z, l0.z);
+         v[3] = atten_one(r.y >> 16, d0.w, l0.w);
+         v[4] = atten_one(r.z & 0xFFFFu, d1.x, l1.x);
+         v[5] = atten_one(r.z >> 16, d1.y, l1.y);
+         v[6] = atten_one(r.w & 0xFFFFu, d1.z, l1.z);
+         v[7] = atten_one(r.w >> 16, d1.w, l1.w);
+         if (cfg.mask) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+               if (!mask_keep(cfg.mask, cfg.wpr, y, x + j)) v[j] = 0.f;
+         }
+         float4* o = reinterpret_cast<float4*>(dst + i8);
+         __stcs(o, make_float4(v[0], v[1], v[2], v[3]));
+         __stcs(o + 1, make_float4(v[4], v[5], v[6], v[7]));
+      }
+   } else {
+      for (int i = threadIdx.x; i < n; i += kThreads) {
+         const int x = i % D;
+         float v = atten_one(tile[i], __ldg(dk + x), __ldg(ld + i));
+         if (!mask_keep(cfg.mask, cfg.wpr, y0 + i / D, x)) v = 0.f;
+         __stcs(dst + i, v);
+      }
    }
 }
 
@@ -177,6 +209,18 @@ __global__ void dark_average(const uint16_t* __restrict__ frames, int n, int L, 
    dark[k * D + d] = (float)__ddiv_rn(acc, __dmul_rn((double)n, (double)P));
 }
 
+// Reordering (Reordering.cu:195-204): module-major -> detector-major, one
+// thread per output sample (consecutive threads write consecutive detectors).
+__global__ void reorder(const uint16_t* __restrict__ in, uint16_t* __restrict__ out, int modules,
+                        int P, int D) {
+   const size_t fs = (size_t)P * D;
+   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= fs) return;
+   const int y = (int)(i / D), x = (int)(i % D);
+   const size_t b = blockIdx.y;
+   out[b * fs + i] = __ldg(in + b * fs + raw_offset(y, x, P, D, modules));
+}
+
 __global__ void logden_table(const float* __restrict__ avg, const float* __restrict__ dark, int P,
                              int D, float* __restrict__ logden) {
    const size_t fs = (size_t)P * D;
@@ -204,7 +248,7 @@ cudaError_t launch_attenuation(const uint16_t* raw, float* out, int batch,
       dim3 grid((cfg.P + kRows - 1) / kRows, batch);
       attenuation_repair<<<grid, kThreads, smem, st>>>(raw, out, cfg, runs->counts, runs->runs,
                                                        max_runs);
-   } else if (cfg.D % 8 == 0) {
+   } else if (cfg.D % 8 == 0 && (cfg.modules <= 0 || (cfg.D / cfg.modules) % 8 == 0)) {
       dim3 grid((unsigned)((fs / 8 + kThreads - 1) / kThreads), batch);
       attenuation_vec8<<<grid, kThreads, 0, st>>>(raw, out, cfg);
    } else {
@@ -226,6 +270,15 @@ cudaError_t launch_dark_average(const uint16_t* frames, int n, int L, int P, int
                                 float* dark, cudaStream_t st) {
    dim3 grid((D + 127) / 128, L);
    dark_average<<<grid, 128, 0, st>>>(frames, n, L, P, D, quirk, dark);
+   return cudaGetLastError();
+}
+
+cudaError_t launch_reorder(const uint16_t* in, uint16_t* out, int modules, int P, int D, int batch,
+                           cudaStream_t st) {
+   if (batch <= 0) return cudaSuccess;
+   const size_t fs = (size_t)P * D;
+   dim3 grid((unsigned)((fs + 255) / 256), batch);
+   reorder<<<grid, 256, 0, st>>>(in, out, modules, P, D);
    return cudaGetLastError();
 }
 

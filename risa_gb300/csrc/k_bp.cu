@@ -93,10 +93,13 @@ __global__ void __launch_bounds__(TX*(TY / PPT)) bp_tile(const float* __restrict
          s_w0[threadIdx.x] = w0;
       }
       __syncthreads();
-      for (int i = threadIdx.x; i < na * wlen; i += NT) {
-         const int ai = i / wlen, m = i - ai * wlen;
-         const int k = s_w0[ai] + m;
-         win[i] = (k >= 0 && k < Dp) ? __ldg(q + (size_t)(c0 + ai) * Dp + k) : 0.f;
+      for (int ai = threadIdx.x / 32; ai < na; ai += NT / 32) {
+         const int w0 = s_w0[ai];
+         const float* row = q + (size_t)(c0 + ai) * Dp;
+         for (int m = threadIdx.x % 32; m < wlen; m += 32) {
+            const int k = w0 + m;
+            win[ai * wlen + m] = (k >= 0 && k < Dp) ? __ldg(row + k) : 0.f;
+         }
       }
       __syncthreads();
 #pragma unroll 4
@@ -223,18 +226,23 @@ __global__ void __launch_bounds__(256) bp_linear_pairs(const float* __restrict__
          s_w0[threadIdx.x] = w0;
       }
       __syncthreads();
-      const int per_slice = na * wlen;
-      for (int i = threadIdx.x; i < S * per_slice; i += NT) {
-         const int si = i / per_slice, rem = i - si * per_slice;
-         const int ai = rem / wlen, m = rem - ai * wlen;
-         const int k = s_w0[ai] + m;
-         float q0 = 0.f, q1 = 0.f;
-         if (s0 + si < batch) {
-            const float* row = sino + ((size_t)(s0 + si) * Pp + c0 + ai) * Dp;
-            if (k >= 0 && k < Dp) q0 = __ldg(row + k);
-            if (k + 1 >= 0 && k + 1 < Dp) q1 = __ldg(row + k + 1);
+      // one warp per (slice, angle) window, lanes along the bins: coalesced
+      // loads, no per-element division
+      for (int rowi = warp; rowi < S * na; rowi += NT / 32) {
+         const int si = rowi / na, ai = rowi - si * na;
+         const int w0 = s_w0[ai];
+         float2* dst = wsm + (si * ACH + ai) * wlen;
+         const bool live = s0 + si < batch;
+         const float* row = sino + ((size_t)(s0 + si) * Pp + c0 + ai) * Dp;
+         for (int m = lane; m < wlen; m += 32) {
+            const int k = w0 + m;
+            float q0 = 0.f, q1 = 0.f;
+            if (live) {
+               if (k >= 0 && k < Dp) q0 = __ldg(row + k);
+               if (k + 1 >= 0 && k + 1 < Dp) q1 = __ldg(row + k + 1);
+            }
+            dst[m] = make_float2(0.5f * (q0 + q1), q1 - q0);
          }
-         wsm[(si * ACH + ai) * wlen + m] = make_float2(0.5f * (q0 + q1), q1 - q0);
       }
       __syncthreads();
 #pragma unroll 2

@@ -35,19 +35,21 @@ __global__ void defect_stats_init(ColStats* st, int n) {
 // grid: x = column blocks, y = row chunks, z = frame. One thread per column.
 __global__ void __launch_bounds__(kStatThreads) defect_stats(const uint16_t* __restrict__ frames,
                                                              ColStats* __restrict__ st, int P,
-                                                             int D) {
+                                                             int D, int modules) {
    const int d = blockIdx.x * kStatThreads + threadIdx.x;
    if (d >= D) return;
    const int r0 = blockIdx.y * kStatRows;
    const int r1 = min(r0 + kStatRows, P - 1);  // pairs (p, p+1) with p <= P-2
    if (r0 >= r1) return;
-   const uint16_t* f = frames + (size_t)blockIdx.z * P * D + d;
-   unsigned int prev = __ldg(f + (size_t)r0 * D);
+   // a column is strided by D (detector-major) or by the module width (module-major)
+   const size_t rs = modules > 0 ? (size_t)(D / modules) : (size_t)D;
+   const uint16_t* f = frames + (size_t)blockIdx.z * P * D + raw_offset(0, d, P, D, modules);
+   unsigned int prev = __ldg(f + (size_t)r0 * rs);
    unsigned int mx = prev, mn = prev;
    unsigned long long tv = 0ull;
 #pragma unroll 8
    for (int p = r0; p < r1; ++p) {
-      const unsigned int next = __ldg(f + (size_t)(p + 1) * D);
+      const unsigned int next = __ldg(f + (size_t)(p + 1) * rs);
       tv += (prev > next) ? (prev - next) : (next - prev);
       mx = max(mx, prev);
       mn = min(mn, prev);
@@ -165,27 +167,14 @@ __global__ void defect_repair(uint16_t* __restrict__ frames, DefectCfg cfg,
    const int f = blockIdx.y;
    if (p >= cfg.P) return;
    const int n = counts[f];
-   uint16_t* row = frames + ((size_t)f * cfg.P + p) * cfg.D;
+   uint16_t* fr = frames + (size_t)f * cfg.P * cfg.D;
+   auto at = [&](int x) -> uint16_t& { return fr[raw_offset(p, x, cfg.P, cfg.D, cfg.modules)]; };
    const DefectRun* rl = runs + (size_t)f * cfg.max_runs;
    for (int r = 0; r < n; ++r) {
       const DefectRun run = rl[r];
       for (int m = 0; m < run.len; ++m) {
          const int col = (run.start + m) % cfg.D;
-         uint16_t val;
-         if (cfg.quirk == RISA_GB_QUIRKS_RISA) {
-            const float w1 = (float)__ddiv_rn((double)m + 1.0, (double)run.len + 1.0);
-            const float w0 = (float)__dsub_rn(1.0, (double)w1);
-            const float v = __fadd_rn(__fmul_rn(w0, (float)row[run.left]),
-                                      __fmul_rn(w1, (float)row[run.right]));
-            val = (uint16_t)__float2uint_rz(v);
-         } else {
-            const double w1 = __ddiv_rn((double)(m + 1), (double)(run.len + 1));
-            const double w0 = __dsub_rn(1.0, w1);
-            const double v = __dadd_rn(__dmul_rn(w0, (double)row[run.left]),
-                                       __dmul_rn(w1, (double)row[run.right]));
-            val = (uint16_t)floor(v + 0.5);
-         }
-         row[col] = val;
+         at(col) = defect_value(at(run.left), at(run.right), m, run.len, cfg.quirk);
       }
    }
 }
@@ -233,7 +222,7 @@ cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const Defect
    defect_stats_init<<<(n + 255) / 256, 256, 0, st>>>(ws.stats, n);
    dim3 grid((cfg.D + kStatThreads - 1) / kStatThreads, (cfg.P - 1 + kStatRows - 1) / kStatRows,
              batch);
-   defect_stats<<<grid, kStatThreads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D);
+   defect_stats<<<grid, kStatThreads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D, cfg.modules);
    const size_t smem = sizeof(double) * cfg.D + sizeof(int) * (cfg.D + 1);
    defect_flags<<<batch, 256, smem, st>>>(ws.stats, cfg, flags_out, ws.counts, ws.runs);
    return cudaGetLastError();

@@ -28,7 +28,42 @@ struct DefectCfg {
    double thresh_min, thresh_max;
    int quirk;
    int max_runs;  // per frame (D/2 + 2)
+   int modules;   // 0: detector-major frames; > 0: module-major with this many modules
 };
+
+// Offset of sample (projection y, detector x) in a raw frame: detector-major
+// [P][D], or module-major [modules][P][D/modules] as the reference's loader
+// delivers frames (OfflineLoader.cu:56-78).
+__host__ __device__ inline size_t raw_offset(int y, int x, int P, int D, int modules) {
+   if (modules <= 0) return (size_t)y * D + x;
+   const int w = D / modules, m = x / w;
+   return ((size_t)m * P + y) * w + (x - m * w);
+}
+cudaError_t launch_reorder(const uint16_t* in, uint16_t* out, int modules, int P, int D, int batch,
+                           cudaStream_t st);
+
+#ifdef __CUDACC__
+// Repaired value of element m of a defect run of length len from its left and
+// right neighbours (interpolationFunctions.h:86-92): w1 = (m+1)/(len+1),
+// w0 = 1 - w1, v = w0*left + w1*right in float, each operation rounded on its
+// own. The reference forms w1 as a double quotient rounded to float; for
+// integer operands below 2^16 the quotient is never within 2^-41 (relative)
+// of a float rounding midpoint unless it equals one, so the single IEEE float
+// division gives the same bits without FP64 arithmetic. RISA mode truncates
+// to uint16 as the reference's conversion does; NONE mode rounds to nearest.
+__device__ __forceinline__ uint16_t defect_value(unsigned left, unsigned right, int m, int len,
+                                                 int quirk) {
+   const float w1 = __fdiv_rn((float)(m + 1), (float)(len + 1));
+   const float w0 = __fsub_rn(1.0f, w1);
+   const float v = __fadd_rn(__fmul_rn(w0, (float)left), __fmul_rn(w1, (float)right));
+   if (quirk == 1) return (uint16_t)__float2uint_rz(v);
+   return (uint16_t)__float2uint_rz(floorf(__fadd_rn(v, 0.5f)));
+}
+template <class Row>
+__device__ __forceinline__ uint16_t repair_value(const Row& row, const DefectRun& run, int m, int quirk) {
+   return defect_value(row[run.left], row[run.right], m, run.len, quirk);
+}
+#endif
 size_t defects_workspace_bytes(int D, int batch, int max_runs);
 // Workspace layout: [batch*D ColStats][batch int run counts][batch*max_runs DefectRun]
 struct DefectWorkspace {
@@ -53,6 +88,7 @@ struct AttenuationCfg {
    const uint32_t* mask;  // relevant-area bits [P][wpr] or nullptr
    int wpr;
    int quirk;
+   int modules;           // raw layout, see raw_offset
 };
 // With runs != nullptr the defect repair of each frame is applied on the fly.
 cudaError_t launch_attenuation(const uint16_t* raw, float* out, int batch,

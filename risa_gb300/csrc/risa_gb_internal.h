@@ -39,6 +39,7 @@ struct Params {
    double masking_value = 0.0;
    int normalize = 0;
    int repair_reference = 1;
+   int module_major = 0;
 };
 risa_gb_status import_geometry(const risa_gb_geometry* g, Geometry* out, bool need_fan,
                                bool need_par, bool need_image);
@@ -84,5 +85,6 @@ void build_relevant_mask_bits(const Geometry& g, const Params& p, std::vector<ui
 
 // ---------------------------------------------------------------- config file
 risa_gb_status load_config(const char* path, risa_gb_geometry* g, risa_gb_params* p);
+risa_gb_status lookup_config(const char* path, const char* key, char* value, size_t value_len);
 
 }  // namespace risa_gb
