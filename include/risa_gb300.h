@@ -209,6 +209,38 @@ risa_gb_status risa_gb_filter_enqueue(risa_gb_filter* h, float* sino, int batch,
 /* FFT length and the frequency response H[len/2+1] (host copy). */
 risa_gb_status risa_gb_filter_response(const risa_gb_filter* h, int* len, float* host_h);
 risa_gb_status risa_gb_filter_destroy(risa_gb_filter* h);
+/* A filter given by real spatial taps instead of a window: y[n] = sum_j
+ * taps[j] * x[n - (j - n_taps/2)] (linear convolution, zero outside the row).
+ * The FFT length is params->pad, or the next power of two >= n_par_det +
+ * n_taps - 1 when pad is 0; the frequency response is built in FP64. */
+risa_gb_status risa_gb_filter_create_taps(const risa_gb_geometry* g, const risa_gb_params* p,
+                                          const float* taps, int n_taps, risa_gb_filter** out);
+/* The transposed filter (correlation with the taps), in place. */
+risa_gb_status risa_gb_filter_enqueue_adjoint(risa_gb_filter* h, float* sino, int batch,
+                                              void* stream);
+/* Gradient of a loss with respect to the taps of a taps-defined filter:
+ * grad[j] = sum over rows and n of g[n] * x[n - (j - n_taps/2)], for the filter
+ * input x and the gradient g at its output (both [batch][Pp][Dp] device).
+ * grad: device float[n_taps]. */
+size_t risa_gb_filter_taps_grad_workspace_bytes(const risa_gb_filter* h, int batch);
+risa_gb_status risa_gb_filter_taps_grad(risa_gb_filter* h, const float* x, const float* g,
+                                        float* grad, int batch, void* workspace, void* stream);
+/* The same window-designed filter evaluated as a dense Toeplitz contraction
+ * Y = X T on the tensor cores (tcgen05, bf16 split in three terms, FP32
+ * accumulation in tensor memory): T[k][n] = c[(n - k) mod len] with c the
+ * inverse DFT of the frequency response, built and split in FP64. Needs
+ * n_par_det % 128 == 0. The enqueue filters [batch][Pp][Dp] rows in place and
+ * needs risa_gb_toeplitz_workspace_bytes of device workspace. */
+typedef struct risa_gb_toeplitz risa_gb_toeplitz;
+risa_gb_status risa_gb_toeplitz_create(const risa_gb_geometry* g, const risa_gb_params* p,
+                                       risa_gb_toeplitz** out);
+size_t risa_gb_toeplitz_workspace_bytes(const risa_gb_toeplitz* h, int batch);
+risa_gb_status risa_gb_toeplitz_enqueue(risa_gb_toeplitz* h, float* sino, int batch,
+                                        void* workspace, void* stream);
+/* Synchronises and returns RISA_GB_ETIMEDOUT if a bounded device-side wait of
+ * an earlier enqueue ran out (the kernel then skipped its output). */
+risa_gb_status risa_gb_toeplitz_check(risa_gb_toeplitz* h);
+risa_gb_status risa_gb_toeplitz_destroy(risa_gb_toeplitz* h);
 /* Host-only filter design (no GPU). h: len/2 + 1 floats. */
 risa_gb_status risa_gb_filter_design_host(const risa_gb_geometry* g, const risa_gb_params* p,
                                           int* len, float* h);

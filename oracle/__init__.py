@@ -103,6 +103,8 @@ def lib():
             "orc_mask": (None, [vp, i, d, i]),
             "orc_fbp": (i, [vp, vp, vp, vp, vp, vp, vp, vp, i, vp, i]),
             "orc_fbp_parallel": (i, [vp, vp, vp, i, vp, i]),
+            "orc_filter_rows_taps": (i, [vp, i, i, vp, i]),
+            "orc_fbp_parallel_taps": (i, [vp, vp, vp, i, vp, i, vp, i]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(_lib, name)
@@ -332,6 +334,27 @@ def fbp(geom, params: FbpParams, rec: F2PRecords, ref, dark, raw, planes, releva
     out = np.zeros((n, g.n_pixels, g.n_pixels), np.float64)
     _check(lib().orc_fbp(ctypes.byref(g), ctypes.byref(params), ctypes.byref(rec._c), _p(ref),
                          _p(dark), _p(m), _p(raw), _p(planes), n, _p(out), n_threads), "fbp")
+    return out
+
+
+def filter_rows_taps(rows: np.ndarray, taps: np.ndarray) -> np.ndarray:
+    out = np.array(rows, dtype=np.float64, copy=True, order="C")
+    R, Dp = out.shape
+    t = np.ascontiguousarray(taps, dtype=np.float64)
+    _check(lib().orc_filter_rows_taps(_p(out), R, Dp, _p(t), len(t)), "filter_rows_taps")
+    return out
+
+
+def fbp_parallel_taps(geom, params: FbpParams, sino: np.ndarray, taps: np.ndarray,
+                      n_threads: int = 0) -> np.ndarray:
+    """Filter by taps, backproject (and mask per params) parallel sinograms [n, Pp, Dp], FP64."""
+    g = make_geometry(geom)
+    sino = np.ascontiguousarray(sino, dtype=np.float64)
+    t = np.ascontiguousarray(taps, dtype=np.float64)
+    n = sino.shape[0]
+    out = np.zeros((n, g.n_pixels, g.n_pixels), np.float64)
+    _check(lib().orc_fbp_parallel_taps(ctypes.byref(g), ctypes.byref(params), _p(sino), n, _p(t), len(t),
+                                       _p(out), n_threads), "fbp_parallel_taps")
     return out
 
 

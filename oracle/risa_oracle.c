@@ -723,6 +723,26 @@ int orc_filter_rows(double* rows, int n_rows, int Dp, int len, const double* h) 
    return 0;
 }
 
+int orc_filter_rows_taps(double* rows, int n_rows, int Dp, const double* taps, int n_taps) {
+   if (!rows || !taps || n_taps < 1 || Dp < 1) return -1;
+   const int c = n_taps / 2;
+   double* x = (double*)malloc(sizeof(double) * Dp);
+   for (int r = 0; r < n_rows; ++r) {
+      double* y = rows + (size_t)r * Dp;
+      memcpy(x, y, sizeof(double) * Dp);
+      for (int n = 0; n < Dp; ++n) {
+         double acc = 0.0;
+         for (int j = 0; j < n_taps; ++j) {
+            const int m = n - (j - c);
+            if (m >= 0 && m < Dp) acc += taps[j] * x[m];
+         }
+         y[n] = acc;
+      }
+   }
+   free(x);
+   return 0;
+}
+
 /* ========================================================================== */
 /* Backprojection                                                               */
 /* ========================================================================== */
@@ -818,12 +838,17 @@ typedef struct {
    double* out;
    const double* h;
    int len;
+   const double* taps;
+   int n_taps;
    int rc;
 } orc_job;
 
 static void finish_slice(const orc_job* jb, double* par, double* img) {
    const orc_geometry* g = jb->g;
-   orc_filter_rows(par, g->n_par_proj, g->n_par_det, jb->len, jb->h);
+   if (jb->taps)
+      orc_filter_rows_taps(par, g->n_par_proj, g->n_par_det, jb->taps, jb->n_taps);
+   else
+      orc_filter_rows(par, g->n_par_proj, g->n_par_det, jb->len, jb->h);
    orc_backproject(par, g->n_par_proj, g->n_par_det, g->n_pixels, g->rotation_offset,
                    jb->p->interp, jb->p->quirk, img);
    if (jb->p->masking || jb->p->normalize) {
@@ -923,5 +948,16 @@ int orc_fbp_parallel(const orc_geometry* g, const orc_fbp_params* p, const doubl
    jb.h = h;
    run_jobs(&jb, n_threads);
    free(h);
+   return 0;
+}
+
+int orc_fbp_parallel_taps(const orc_geometry* g, const orc_fbp_params* p, const double* sino,
+                          int n_slices, const double* taps, int n_taps, double* out, int n_threads) {
+   if (!g || !p || !sino || !out || !taps || n_taps < 1 || n_slices < 0) return -1;
+   orc_job jb;
+   memset(&jb, 0, sizeof(jb));
+   jb.g = g; jb.p = p; jb.par_in = sino; jb.n_slices = n_slices; jb.out = out;
+   jb.taps = taps; jb.n_taps = n_taps;
+   run_jobs(&jb, n_threads);
    return 0;
 }

@@ -146,6 +146,11 @@ int orc_design_filter(int len, int filter_type, double cutoff, int quirk, double
 /* rows: [n_rows][n_par_det], filtered in place (zero padding to len). */
 int orc_filter_rows(double* rows, int n_rows, int n_par_det, int len, const double* h);
 
+/* Filtering by real spatial taps (the differentiable filter of this build):
+ * y[n] = sum_j taps[j] * x[n - (j - n_taps/2)], zero outside [0, Dp). Direct
+ * convolution in FP64; rows are filtered in place. */
+int orc_filter_rows_taps(double* rows, int n_rows, int n_par_det, const double* taps, int n_taps);
+
 /* ---- backprojection (a12-a14) ---------------------------------------------- */
 int orc_backproject(const double* sino, int n_par_proj, int n_par_det, int n_pixels,
                     double rotation_offset, int interp, int quirk, double* img);
@@ -175,9 +180,13 @@ int orc_fbp(const orc_geometry* g, const orc_fbp_params* p, const orc_f2p_record
             const float* ref, const float* dark, const float* mask, const uint16_t* raw,
             const int* planes, int n_slices, double* out, int n_threads);
 
-/* Parallel-beam only chain (filter + backprojection + mask) for parallel sinograms. */
+/* Parallel-beam only chain (filter + backprojection + mask) for parallel sinograms.
+ * With taps != NULL the rows are filtered by orc_filter_rows_taps instead of the
+ * designed filter. */
 int orc_fbp_parallel(const orc_geometry* g, const orc_fbp_params* p, const double* sino,
                      int n_slices, double* out, int n_threads);
+int orc_fbp_parallel_taps(const orc_geometry* g, const orc_fbp_params* p, const double* sino,
+                          int n_slices, const double* taps, int n_taps, double* out, int n_threads);
 
 #ifdef __cplusplus
 }

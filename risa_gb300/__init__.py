@@ -91,6 +91,15 @@ SIGNATURES = {
     "risa_gb_filter_response": (_i, [_vp, ctypes.POINTER(ctypes.c_int), _vp]),
     "risa_gb_filter_destroy": (_i, [_vp]),
     "risa_gb_filter_design_host": (_i, [_vp, _vp, ctypes.POINTER(ctypes.c_int), _vp]),
+    "risa_gb_filter_create_taps": (_i, [_vp, _vp, _vp, _i, _pp]),
+    "risa_gb_filter_enqueue_adjoint": (_i, [_vp, _vp, _i, _vp]),
+    "risa_gb_filter_taps_grad_workspace_bytes": (_sz, [_vp, _i]),
+    "risa_gb_filter_taps_grad": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp]),
+    "risa_gb_toeplitz_create": (_i, [_vp, _vp, _pp]),
+    "risa_gb_toeplitz_workspace_bytes": (_sz, [_vp, _i]),
+    "risa_gb_toeplitz_enqueue": (_i, [_vp, _vp, _i, _vp, _vp]),
+    "risa_gb_toeplitz_check": (_i, [_vp]),
+    "risa_gb_toeplitz_destroy": (_i, [_vp]),
     "risa_gb_backprojection_create": (_i, [_vp, _vp, _pp]),
     "risa_gb_backprojection_enqueue": (_i, [_vp, _vp, _vp, _i, _vp]),
     "risa_gb_backprojection_enqueue_adjoint": (_i, [_vp, _vp, _vp, _i, _vp]),
@@ -332,13 +341,32 @@ def fan2para_tables_host(geom: Geometry, params: Params, plane: int = 0):
 class Filter(_Handle):
     _destroy = "risa_gb_filter_destroy"
 
-    def __init__(self, geom: Geometry, params: Params):
+    def __init__(self, geom: Geometry, params: Params, taps=None):
+        """Window-designed filter from params, or (taps: host float32 array) a taps-defined one."""
         super().__init__()
-        _check(lib().risa_gb_filter_create(ctypes.byref(geom), ctypes.byref(params), ctypes.byref(self._h)),
-               "filter_create")
+        if taps is None:
+            _check(lib().risa_gb_filter_create(ctypes.byref(geom), ctypes.byref(params), ctypes.byref(self._h)),
+                   "filter_create")
+        else:
+            import numpy as np
+            t = np.ascontiguousarray(taps, dtype=np.float32)
+            _check(lib().risa_gb_filter_create_taps(ctypes.byref(geom), ctypes.byref(params), ptr(t), len(t),
+                                                    ctypes.byref(self._h)), "filter_create_taps")
+            self.n_taps = len(t)
 
     def enqueue(self, sino, batch: int, stream=None):
         _check(lib().risa_gb_filter_enqueue(self._h, ptr(sino), batch, stream_ptr(stream)), "filter_enqueue")
+
+    def enqueue_adjoint(self, sino, batch: int, stream=None):
+        _check(lib().risa_gb_filter_enqueue_adjoint(self._h, ptr(sino), batch, stream_ptr(stream)),
+               "filter_enqueue_adjoint")
+
+    def taps_grad_workspace_bytes(self, batch: int) -> int:
+        return lib().risa_gb_filter_taps_grad_workspace_bytes(self._h, batch)
+
+    def taps_grad(self, x, g, grad, batch: int, workspace, stream=None):
+        _check(lib().risa_gb_filter_taps_grad(self._h, ptr(x), ptr(g), ptr(grad), batch, ptr(workspace),
+                                              stream_ptr(stream)), "filter_taps_grad")
 
     def response(self):
         import numpy as np
@@ -347,6 +375,26 @@ class Filter(_Handle):
         h = np.zeros(n.value // 2 + 1, np.float32)
         _check(lib().risa_gb_filter_response(self._h, ctypes.byref(n), ptr(h)), "filter_response")
         return n.value, h
+
+
+class Toeplitz(_Handle):
+    """The window-designed filter as a split-bf16 tensor-core Toeplitz GEMM (tcgen05)."""
+    _destroy = "risa_gb_toeplitz_destroy"
+
+    def __init__(self, geom: Geometry, params: Params):
+        super().__init__()
+        _check(lib().risa_gb_toeplitz_create(ctypes.byref(geom), ctypes.byref(params), ctypes.byref(self._h)),
+               "toeplitz_create")
+
+    def workspace_bytes(self, batch: int) -> int:
+        return lib().risa_gb_toeplitz_workspace_bytes(self._h, batch)
+
+    def enqueue(self, sino, batch: int, workspace, stream=None):
+        _check(lib().risa_gb_toeplitz_enqueue(self._h, ptr(sino), batch, ptr(workspace), stream_ptr(stream)),
+               "toeplitz_enqueue")
+
+    def check(self):
+        _check(lib().risa_gb_toeplitz_check(self._h), "toeplitz_check")
 
 
 def filter_design_host(geom: Geometry, params: Params):

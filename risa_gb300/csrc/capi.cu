@@ -3,7 +3,9 @@
 // reference's stage classes (see include/risa_gb300.h for the mapping).
 #include "kernels.h"
 #include "risa_gb_internal.h"
+#include "toeplitz.h"
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -212,16 +214,30 @@ struct risa_gb_filter {
    Geometry g;
    Params p;
    int len = 0;
-   std::vector<float> h_host;
-   DevBuf h, tw;
-   FilterCfg cfg() const {
+   std::vector<float> h_host;  // real response [len/2+1] of a window-designed filter
+   int n_taps = 0;             // > 0 for a taps-defined filter
+   DevBuf h, tw;               // complex response [len], twiddles [len]
+   FilterCfg cfg(bool adjoint = false) const {
       FilterCfg c;
       c.rows = g.Pp; c.Dp = g.Dp; c.len = len;
       c.twiddle = tw.as<float2>();
-      c.h = h.as<float>();
+      c.h = h.as<float2>();
+      c.adjoint = adjoint ? 1 : 0;
       return c;
    }
 };
+
+namespace {
+std::vector<float> twiddles(int len) {
+   std::vector<float> tw(2 * (size_t)len);  // interleaved (re, im) of exp(-2 pi i k / len), k < len
+   for (int k = 0; k < len; ++k) {
+      const double ang = -2.0 * 3.14159265358979323846 * (double)k / (double)len;
+      tw[2 * k] = (float)std::cos(ang);
+      tw[2 * k + 1] = (float)std::sin(ang);
+   }
+   return tw;
+}
+}  // namespace
 
 struct risa_gb_backprojection {
    Geometry g;
@@ -629,15 +645,72 @@ risa_gb_status risa_gb_filter_create(const risa_gb_geometry* gi, const risa_gb_p
    RG_TRY(import_geometry(gi, &h->g, false, true, false));
    RG_TRY(import_params(pi, &h->p));
    RG_TRY(design_filter(h->g, h->p, &h->len, &h->h_host));
-   std::vector<float> tw(2 * (size_t)h->len);  // interleaved (re, im) of exp(-2 pi i k / len), k < len
-   for (int k = 0; k < h->len; ++k) {
-      const double ang = -2.0 * 3.14159265358979323846 * (double)k / (double)h->len;
-      tw[2 * k] = (float)std::cos(ang);
-      tw[2 * k + 1] = (float)std::sin(ang);
-   }
-   RG_TRY(h->tw.upload(tw));
-   RG_TRY(h->h.upload(h->h_host));
+   RG_TRY(h->tw.upload(twiddles(h->len)));
+   std::vector<float> hc(2 * (size_t)h->len, 0.f);  // real, even response as complex
+   for (int k = 0; k < h->len; ++k) hc[2 * k] = h->h_host[k <= h->len / 2 ? k : h->len - k];
+   RG_TRY(h->h.upload(hc));
    *out = h.release();
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_filter_create_taps(const risa_gb_geometry* gi, const risa_gb_params* pi, const float* taps,
+                                          int n_taps, risa_gb_filter** out) {
+   if (!out || !taps || n_taps < 1) return fail(RISA_GB_EINVAL, "null output or taps");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_filter> h(new (std::nothrow) risa_gb_filter());
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, false, true, false));
+   RG_TRY(import_params(pi, &h->p));
+   int len = h->p.pad;
+   if (len <= 0) {
+      len = 32;
+      while (len < h->g.Dp + n_taps - 1) len <<= 1;
+   }
+   if ((len & (len - 1)) || len < 32 || len > 8192 || len < h->g.Dp + n_taps - 1)
+      return fail(RISA_GB_EUNSUPPORTED, "taps filter: FFT length must be a power of two in [32, 8192] "
+                                        "and >= n_par_det + n_taps - 1");
+   h->len = len;
+   h->n_taps = n_taps;
+   // H[k] = (1/len) sum_j taps[j] exp(-2 pi i k (j - c) / len), c = n_taps / 2, in FP64
+   const int c = n_taps / 2;
+   std::vector<float> hc(2 * (size_t)len);
+   const double tp = 2.0 * 3.14159265358979323846;
+   for (int k = 0; k < len; ++k) {
+      double re = 0.0, im = 0.0;
+      for (int j = 0; j < n_taps; ++j) {
+         const long m = ((long)k * (long)(j - c)) % len;
+         const double ang = -tp * (double)m / (double)len;
+         re += (double)taps[j] * std::cos(ang);
+         im += (double)taps[j] * std::sin(ang);
+      }
+      hc[2 * k] = (float)(re / len);
+      hc[2 * k + 1] = (float)(im / len);
+   }
+   RG_TRY(h->tw.upload(twiddles(len)));
+   RG_TRY(h->h.upload(hc));
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_filter_enqueue_adjoint(risa_gb_filter* h, float* sino, int batch, void* stream) {
+   if (!h || !sino) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (batch < 0) return fail(RISA_GB_EINVAL, "negative batch");
+   RG_CUDA(launch_filter(sino, batch, h->cfg(true), S(stream)));
+   return RISA_GB_OK;
+}
+
+size_t risa_gb_filter_taps_grad_workspace_bytes(const risa_gb_filter* h, int batch) {
+   if (!h || batch < 1) return 0;
+   return filter_grad_workspace_bytes(h->cfg(), batch);
+}
+
+risa_gb_status risa_gb_filter_taps_grad(risa_gb_filter* h, const float* x, const float* g, float* grad, int batch,
+                                        void* workspace, void* stream) {
+   if (!h || !x || !g || !grad || !workspace) return fail(RISA_GB_EINVAL, "null handle or buffer");
+   if (h->n_taps < 1) return fail(RISA_GB_EINVAL, "the filter was not created from taps");
+   if (batch < 1) return fail(RISA_GB_EINVAL, "batch must be >= 1");
+   RG_CUDA(launch_filter_taps_grad(x, g, batch, h->cfg(), static_cast<float2*>(workspace), h->n_taps,
+                                   h->n_taps / 2, grad, S(stream)));
    return RISA_GB_OK;
 }
 
@@ -988,5 +1061,95 @@ risa_gb_status risa_gb_fbp_intermediates(risa_gb_fbp* h, float** fan, float** pa
 }
 
 risa_gb_backprojection* risa_gb_fbp_backprojection(risa_gb_fbp* h) { return h ? h->bp : nullptr; }
+
+// ---------------------------------------------------------------------------- Toeplitz filter
+struct risa_gb_toeplitz {
+   Geometry g;
+   Params p;
+   int len = 0;
+   DevBuf th, tl, err;
+};
+
+risa_gb_status risa_gb_toeplitz_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                       risa_gb_toeplitz** out) {
+   if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_toeplitz> h(new (std::nothrow) risa_gb_toeplitz());
+   if (!h) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   RG_TRY(import_geometry(gi, &h->g, false, true, false));
+   RG_TRY(import_params(pi, &h->p));
+   const int Dp = h->g.Dp;
+   if (Dp % 128) return fail(RISA_GB_EUNSUPPORTED, "Toeplitz filter needs n_par_det % 128 == 0");
+   std::vector<float> hr;
+   RG_TRY(design_filter(h->g, h->p, &h->len, &hr));
+   const int len = h->len;
+   // c[d] = sum_k H[k] exp(2 pi i k d / len) (H real and even, 1/len included in H)
+   std::vector<double> c(len);
+   const double tp = 2.0 * 3.14159265358979323846;
+   for (int d = 0; d < len; ++d) {
+      double s = 0.0;
+      for (int k = 0; k < len; ++k) {
+         const double hk = hr[k <= len / 2 ? k : len - k];
+         if (hk != 0.0) s += hk * std::cos(tp * (double)(((long)k * d) % len) / (double)len);
+      }
+      c[d] = s;
+   }
+   // T^T[n][k] = c[(n - k) mod len], split into bf16 hi + lo in FP64
+   std::vector<__nv_bfloat16> th((size_t)Dp * Dp), tl((size_t)Dp * Dp);
+   for (int n = 0; n < Dp; ++n)
+      for (int k = 0; k < Dp; ++k) {
+         const double v = c[((n - k) % len + len) % len];
+         const __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
+         th[(size_t)n * Dp + k] = hi;
+         tl[(size_t)n * Dp + k] = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
+      }
+   RG_TRY(h->th.upload(th));
+   RG_TRY(h->tl.upload(tl));
+   RG_TRY(h->err.alloc(sizeof(int)));
+   RG_CUDA(cudaMemset(h->err.p, 0, sizeof(int)));
+   *out = h.release();
+   return RISA_GB_OK;
+}
+
+size_t risa_gb_toeplitz_workspace_bytes(const risa_gb_toeplitz* h, int batch) {
+   if (!h || batch < 1) return 0;
+   return (size_t)2 * 2 * batch * h->g.Pp * h->g.Dp + 256;
+}
+
+risa_gb_status risa_gb_toeplitz_enqueue(risa_gb_toeplitz* h, float* sino, int batch, void* workspace,
+                                        void* stream) {
+   if (!h || !sino || !workspace) return fail(RISA_GB_EINVAL, "null handle, buffer or workspace");
+   if (batch < 0) return fail(RISA_GB_EINVAL, "negative batch");
+   if ((reinterpret_cast<uintptr_t>(workspace) & 255) || (reinterpret_cast<uintptr_t>(sino) & 15))
+      return fail(RISA_GB_EINVAL, "workspace must be 256-byte and sino 16-byte aligned");
+   ToeplitzArgs a;
+   const size_t n = (size_t)batch * h->g.Pp * h->g.Dp;
+   a.x = sino;
+   a.xh = static_cast<__nv_bfloat16*>(workspace);
+   a.xl = a.xh + ((n + 127) & ~(size_t)127);
+   a.th = h->th.as<__nv_bfloat16>();
+   a.tl = h->tl.as<__nv_bfloat16>();
+   a.y = sino;
+   a.rows = batch * h->g.Pp;
+   a.n = h->g.Dp;
+   a.k = h->g.Dp;
+   a.err = h->err.as<int>();
+   RG_CUDA(launch_toeplitz(a, S(stream)));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_toeplitz_check(risa_gb_toeplitz* h) {
+   if (!h) return fail(RISA_GB_EINVAL, "null handle");
+   RG_CUDA(cudaDeviceSynchronize());
+   int code = 0;
+   RG_CUDA(cudaMemcpy(&code, h->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+   if (code) return fail(RISA_GB_ETIMEDOUT, "Toeplitz kernel: bounded wait ran out (stage " + std::to_string(code) + ")");
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_toeplitz_destroy(risa_gb_toeplitz* h) {
+   delete h;
+   return RISA_GB_OK;
+}
 
 }  // extern "C"

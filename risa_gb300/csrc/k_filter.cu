@@ -127,9 +127,10 @@ __global__ void __launch_bounds__(kThreads) filter_rows(float* __restrict__ sino
    float2* other = spec == x0 ? x1 : x0;
    // filter, conjugate for the inverse: ifft(Z) = conj(fft(conj(Z))) / len (the 1/len is in h)
    for (int k = lt; k < len; k += tpp) {
-      const float h = __ldg(cfg.h + (k <= (len >> 1) ? k : len - k));
-      const float2 z = spec[k];
-      spec[k] = make_float2(z.x * h, -z.y * h);
+      float2 h = __ldg(cfg.h + k);
+      if (cfg.adjoint) h.y = -h.y;
+      const float2 y = cmul(spec[k], h);
+      spec[k] = make_float2(y.x, -y.y);
    }
    __syncthreads();
    float2* res = fft(spec, other, cfg.twiddle, len, lt, tpp);
@@ -138,7 +139,119 @@ __global__ void __launch_bounds__(kThreads) filter_rows(float* __restrict__ sino
       if (has_b) row_b[n] = -res[n].y;
    }
 }
+// ---- gradient with respect to the filter taps ------------------------------------
+// For rows x (filter input) and g (gradient at the filter output), the
+// gradient with respect to the circularly placed taps is the circular
+// cross-correlation sum_n g[n] x[n - t] = ifft(G conj(X))[t] / len. Two rows
+// of each are packed per complex FFT as in the filter; their spectra are
+// separated with X_a[k] = (Z[k] + conj(Z[-k])) / 2, X_b[k] = (Z[k] - conj(Z[-k])) / 2i.
+// Each CTA writes the sum of G conj(X) over its rows; a second kernel adds
+// the partial spectra in a fixed order and inverts.
+__global__ void __launch_bounds__(kThreads) filter_grad_partial(const float* __restrict__ x,
+                                                                const float* __restrict__ g,
+                                                                int total_rows, FilterCfg cfg, int tpp,
+                                                                float2* __restrict__ partial) {
+   extern __shared__ float2 buf[];
+   const int len = cfg.len;
+   const int ppb = kThreads / tpp;
+   const int local = threadIdx.x / tpp, lt = threadIdx.x % tpp;
+   const int pair = blockIdx.x * ppb + local;
+   const int ra = 2 * pair, rb = 2 * pair + 1;
+   const bool has_a = ra < total_rows, has_b = rb < total_rows;
+   float2* bx0 = buf + (size_t)local * 4 * len;
+   float2* bx1 = bx0 + len;
+   float2* bg0 = bx1 + len;
+   float2* bg1 = bg0 + len;
+   float2* acc = buf + (size_t)ppb * 4 * len;  // [len], shared by the CTA's pairs
+   const int Dp = cfg.Dp;
+   for (int n = lt; n < len; n += tpp) {
+      const bool in = n < Dp;
+      bx0[n] = make_float2((has_a && in) ? x[(size_t)ra * Dp + n] : 0.f, (has_b && in) ? x[(size_t)rb * Dp + n] : 0.f);
+      bg0[n] = make_float2((has_a && in) ? g[(size_t)ra * Dp + n] : 0.f, (has_b && in) ? g[(size_t)rb * Dp + n] : 0.f);
+   }
+   for (int k = threadIdx.x; k < len; k += kThreads) acc[k] = make_float2(0.f, 0.f);
+   __syncthreads();
+   float2* zx = fft(bx0, bx1, cfg.twiddle, len, lt, tpp);
+   float2* zg = fft(bg0, bg1, cfg.twiddle, len, lt, tpp);
+   for (int p = 0; p < ppb; ++p) {  // pairs of the CTA add in a fixed order
+      if (local == p) {
+         for (int k = lt; k < len; k += tpp) {
+            const int nk = (len - k) & (len - 1);
+            const float2 zk = zx[k], zn = zx[nk], gk = zg[k], gn = zg[nk];
+            // X_a = (zk + conj zn)/2, X_b = (zk - conj zn)/(2i); same for G
+            const float2 xa = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+            const float2 xb = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+            const float2 ga = make_float2(0.5f * (gk.x + gn.x), 0.5f * (gk.y - gn.y));
+            const float2 gb = make_float2(0.5f * (gk.y + gn.y), -0.5f * (gk.x - gn.x));
+            // G conj(X)
+            const float2 pa = make_float2(ga.x * xa.x + ga.y * xa.y, ga.y * xa.x - ga.x * xa.y);
+            const float2 pb = make_float2(gb.x * xb.x + gb.y * xb.y, gb.y * xb.x - gb.x * xb.y);
+            acc[k].x += pa.x + pb.x;
+            acc[k].y += pa.y + pb.y;
+         }
+      }
+      __syncthreads();
+   }
+   for (int k = threadIdx.x; k < len; k += kThreads) partial[(size_t)blockIdx.x * len + k] = acc[k];
+}
+
+// One CTA: sum the partial spectra in block order, invert, scale by 1/len.
+__global__ void __launch_bounds__(kThreads) filter_grad_finish(const float2* __restrict__ partial,
+                                                               int blocks, FilterCfg cfg, int n_taps,
+                                                               int center, float* __restrict__ grad) {
+   extern __shared__ float2 buf[];
+   const int len = cfg.len;
+   float2* a = buf;
+   float2* b = buf + len;
+   for (int k = threadIdx.x; k < len; k += kThreads) {
+      float2 s = make_float2(0.f, 0.f);
+      for (int j = 0; j < blocks; ++j) {
+         const float2 v = partial[(size_t)j * len + k];
+         s.x += v.x;
+         s.y += v.y;
+      }
+      a[k] = make_float2(s.x, -s.y);  // conj for the inverse
+   }
+   __syncthreads();
+   // one transform spread over the first tpp threads; the others only meet the barriers
+   const int tpp = len / 8 < kThreads ? len / 8 : kThreads;
+   float2* r = fft(a, b, cfg.twiddle, len, threadIdx.x < tpp ? threadIdx.x : len, tpp);
+   const float inv = 1.0f / (float)len;
+   // tap j sits at lag (j - center) mod len; the real part of conj(fft(conj(S))) is ifft(S) * len
+   for (int j = threadIdx.x; j < n_taps; j += kThreads) grad[j] = r[((j - center) % len + len) % len].x * inv;
+}
 }  // namespace
+
+size_t filter_grad_workspace_bytes(const FilterCfg& cfg, int batch) {
+   const int total_rows = batch * cfg.rows;
+   const int tpp = cfg.len / 8 < kThreads ? cfg.len / 8 : kThreads;
+   const int ppb = kThreads / tpp;
+   const int pairs = (total_rows + 1) / 2;
+   const int blocks = (pairs + ppb - 1) / ppb;
+   return sizeof(float2) * (size_t)cfg.len * blocks;
+}
+
+cudaError_t launch_filter_taps_grad(const float* x, const float* g, int batch, const FilterCfg& cfg,
+                                    float2* workspace, int n_taps, int center, float* grad_taps,
+                                    cudaStream_t st) {
+   if (batch <= 0) return cudaSuccess;
+   const int total_rows = batch * cfg.rows;
+   const int tpp = cfg.len / 8 < kThreads ? cfg.len / 8 : kThreads;
+   const int ppb = kThreads / tpp;
+   const int pairs = (total_rows + 1) / 2;
+   const int blocks = (pairs + ppb - 1) / ppb;
+   const size_t smem = sizeof(float2) * ((size_t)4 * cfg.len * ppb + cfg.len);
+   if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+   cudaError_t e = cudaFuncSetAttribute(filter_grad_partial, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem);
+   if (e != cudaSuccess) return e;
+   filter_grad_partial<<<blocks, kThreads, smem, st>>>(x, g, total_rows, cfg, tpp, workspace);
+   const size_t smem2 = sizeof(float2) * 2 * (size_t)cfg.len;
+   e = cudaFuncSetAttribute(filter_grad_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+   if (e != cudaSuccess) return e;
+   filter_grad_finish<<<1, kThreads, smem2, st>>>(workspace, blocks, cfg, n_taps, center, grad_taps);
+   return cudaGetLastError();
+}
 
 cudaError_t launch_filter(float* sino, int batch, const FilterCfg& cfg, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;

@@ -1,0 +1,300 @@
+// Filtering as a dense Toeplitz contraction on the 5th-generation tensor cores.
+//
+// The ramp-family filter is a linear convolution, y[n] = sum_k x[k] c[n - k]
+// (c = inverse DFT of the frequency response, circular over the FFT length),
+// i.e. Y = X T with the Dp x Dp Toeplitz matrix T[k][n] = c[(n - k) mod len]
+// restricted to the detector rows that are non-zero after padding. Rows of
+// every slice form the M dimension. FP32 accuracy comes from a three-term
+// split into bf16: X = Xh + Xl, T = Th + Tl, X T ~ Xh Th + Xh Tl + Xl Th,
+// accumulated in FP32 in tensor memory; T is built and split in FP64 on the
+// host.
+//
+// Kernel structure (one 128 x 128 output tile per CTA, 4 warps):
+//   * warp 0, one lane: TMA producer. Per 64-wide K block it loads the four
+//     operand tiles (Xh, Xl: 128 x 64; Th^T, Tl^T: 128 x 64, all K-major,
+//     128-byte swizzled) into one of kStages shared-memory stages and arms the
+//     stage's "full" mbarrier with the byte count.
+//   * warp 1, one lane: MMA issuer. Waits for a full stage, issues
+//     3 x 4 tcgen05.mma (M128 N128 K16, bf16 in, f32 accumulate in TMEM), and
+//     commits to the stage's "empty" mbarrier so the producer can refill it.
+//     After the last block it commits to the accumulator barrier.
+//   * all 4 warps: epilogue. Each warp reads its 32 TMEM lanes (rows) with
+//     tcgen05.ld and stores FP32 rows.
+// Every mbarrier wait is bounded: on timeout the CTA records an error code,
+// stops issuing work, waits (bounded) for its own outstanding operations and
+// frees its tensor memory before returning.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.h"
+#include "toeplitz.h"
+
+namespace risa_gb {
+
+namespace {
+constexpr int kBM = 128, kBN = 128, kBK = 64, kStages = 3;
+constexpr int kTileBytes = kBM * kBK * 2;                  // 16 KiB per operand tile
+constexpr int kStageBytes = 4 * kTileBytes;                // Xh, Xl, Th, Tl
+constexpr uint32_t kSpinLimit = 1u << 26;                  // ~ seconds of polling
+constexpr uint32_t kTmemCols = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+   return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+   uint32_t ok;
+   asm volatile(
+       "{\n\t.reg .pred p;\n\t"
+       "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+       "selp.u32 %0, 1, 0, p;\n\t}"
+       : "=r"(ok)
+       : "r"(smem_u32(bar)), "r"(parity)
+       : "memory");
+   return ok != 0;
+}
+
+// Bounded wait; returns false (and records the error) when it gives up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+   for (uint32_t i = 0; i < kSpinLimit; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
+   atomicCAS(err, 0, code);
+   return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+   asm volatile(
+       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
+           "r"(smem_u32(dst)),
+       "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+       : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand tile, 128-byte swizzle,
+// 8-row core groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(const void* tile) {
+   const uint64_t addr = smem_u32(tile);
+   uint64_t d = 0;
+   d |= (addr >> 4) & 0x3FFFull;            // start address
+   d |= (uint64_t)1 << 16;                  // leading byte offset (unused with swizzle)
+   d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset
+   d |= (uint64_t)1 << 46;                  // descriptor version
+   d |= (uint64_t)2 << 61;                  // 128-byte swizzle
+   return d;
+}
+
+// Instruction descriptor, kind::f16: bf16 A and B, f32 D, both K-major, M128 N128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
+                            ((uint32_t)(kBM >> 4) << 24);
+
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+   asm volatile(
+       "{\n\t.reg .pred p;\n\t"
+       "setp.ne.b32 p, %4, 0;\n\t"
+       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+       "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+       : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                    smem_u32(bar))
+                : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+   asm volatile(
+       "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+       "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+       "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+         "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+         "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+         "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+       : "r"(taddr));
+   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(128, 1) toeplitz_gemm(const __grid_constant__ CUtensorMap map_xh,
+                                                        const __grid_constant__ CUtensorMap map_xl,
+                                                        const __grid_constant__ CUtensorMap map_th,
+                                                        const __grid_constant__ CUtensorMap map_tl,
+                                                        float* __restrict__ y, int M, int N, int K,
+                                                        int* __restrict__ err) {
+   extern __shared__ __align__(1024) unsigned char smem_raw[];
+   // stages must sit on 1024-byte boundaries for the 128-byte swizzle
+   unsigned char* smem = reinterpret_cast<unsigned char*>(
+       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+   __shared__ __align__(8) uint64_t full_bar[kStages], empty_bar[kStages], accum_bar;
+   __shared__ uint32_t tmem_base_slot;
+   __shared__ int cta_failed;
+
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int n0 = blockIdx.x * kBN, m0 = blockIdx.y * kBM;
+   const int kblocks = K / kBK;
+
+   if (threadIdx.x == 0) {
+      for (int s = 0; s < kStages; ++s) {
+         mbar_init(&full_bar[s], 1);
+         mbar_init(&empty_bar[s], 1);
+      }
+      mbar_init(&accum_bar, 1);
+      cta_failed = 0;
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+   }
+   if (warp == 1) {  // one warp allocates the accumulator columns
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       smem_u32(&tmem_base_slot)),
+                   "r"(kTmemCols)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   const uint32_t tmem_d = tmem_base_slot;
+
+   if (warp == 0) {
+      if (lane == 0) {
+         for (int kb = 0; kb < kblocks; ++kb) {
+            const int s = kb % kStages;
+            const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+            if (!mbar_wait(&empty_bar[s], ph ^ 1u, err, 1)) { cta_failed = 1; break; }
+            unsigned char* st = smem + (size_t)s * kStageBytes;
+            mbar_arrive_expect_tx(&full_bar[s], kStageBytes);
+            const int kx = kb * kBK;  // 64 bf16 = 128 bytes: 16-byte aligned
+            tma_load_2d(st + 0 * kTileBytes, &map_xh, &full_bar[s], kx, m0);
+            tma_load_2d(st + 1 * kTileBytes, &map_xl, &full_bar[s], kx, m0);
+            tma_load_2d(st + 2 * kTileBytes, &map_th, &full_bar[s], kx, n0);
+            tma_load_2d(st + 3 * kTileBytes, &map_tl, &full_bar[s], kx, n0);
+         }
+      }
+      __syncwarp();
+   } else if (warp == 1) {
+      if (lane == 0) {
+         bool ok = true;
+         for (int kb = 0; kb < kblocks && ok; ++kb) {
+            const int s = kb % kStages;
+            const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+            if (!mbar_wait(&full_bar[s], ph, err, 2)) { ok = false; cta_failed = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            unsigned char* st = smem + (size_t)s * kStageBytes;
+            const uint64_t dxh = smem_desc(st), dxl = smem_desc(st + kTileBytes);
+            const uint64_t dth = smem_desc(st + 2 * kTileBytes), dtl = smem_desc(st + 3 * kTileBytes);
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; ++kk) {
+               // advance 16 bf16 (32 bytes) along K inside the swizzle atom
+               const uint64_t o = (uint64_t)((kk * 32) >> 4);
+               const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+               umma_f16(tmem_d, dxh + o, dth + o, acc0);
+               umma_f16(tmem_d, dxh + o, dtl + o, 1u);
+               umma_f16(tmem_d, dxl + o, dth + o, 1u);
+            }
+            umma_commit(&empty_bar[s]);  // the stage is free once these MMAs finish
+         }
+         umma_commit(&accum_bar);  // arrives when every MMA issued above has finished
+      }
+      __syncwarp();
+   }
+
+   // epilogue: each warp owns TMEM lanes (rows) 32w .. 32w+31
+   const bool have = mbar_wait(&accum_bar, 0, err, 3);
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   const int row = m0 + warp * 32 + lane;
+   if (have && !cta_failed) {
+#pragma unroll 1
+      for (int c = 0; c < kBN; c += 32) {
+         uint32_t r[32];
+         tmem_ld32(tmem_d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
+         if (row < M) {
+            float4* dst = reinterpret_cast<float4*>(y + (size_t)row * N + n0 + c);
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+               dst[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
+                                    __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+         }
+      }
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   if (warp == 1) {
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(kTmemCols)
+                   : "memory");
+   }
+}
+
+// fp32 rows -> bf16 (hi, lo) with hi = rn(x), lo = rn(x - hi)
+__global__ void split_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ hi,
+                           __nv_bfloat16* __restrict__ lo, size_t n) {
+   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= n) return;
+   const float v = x[i];
+   const __nv_bfloat16 h = __float2bfloat16_rn(v);
+   hi[i] = h;
+   lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+   static EncodeTiled fn = nullptr;
+   if (!fn) {
+      void* p = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+          q == cudaDriverEntryPointSuccess)
+         fn = reinterpret_cast<EncodeTiled>(p);
+   }
+   return fn;
+}
+
+// bf16 matrix [rows][cols] (cols contiguous), boxes of 64 columns x 128 rows.
+bool make_map(CUtensorMap* map, const void* base, int rows, int cols) {
+   EncodeTiled enc = encode_fn();
+   if (!enc) return false;
+   const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+   const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+   const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+   const cuuint32_t estr[2] = {1, 1};
+   return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
+size_t toeplitz_smem_bytes() { return (size_t)kStages * kStageBytes + 1024; }
+
+cudaError_t launch_toeplitz(const ToeplitzArgs& a, cudaStream_t st) {
+   if (a.rows <= 0) return cudaSuccess;
+   if (a.n % kBN || a.k % kBK) return cudaErrorInvalidValue;
+   const size_t n = (size_t)a.rows * a.k;
+   split_bf16<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a.x, a.xh, a.xl, n);
+   CUtensorMap mxh, mxl, mth, mtl;
+   if (!make_map(&mxh, a.xh, a.rows, a.k) || !make_map(&mxl, a.xl, a.rows, a.k) ||
+       !make_map(&mth, a.th, a.n, a.k) || !make_map(&mtl, a.tl, a.n, a.k))
+      return cudaErrorInvalidValue;
+   const size_t smem = toeplitz_smem_bytes();
+   cudaError_t e = cudaFuncSetAttribute(toeplitz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+   if (e != cudaSuccess) return e;
+   dim3 grid(a.n / kBN, (a.rows + kBM - 1) / kBM);
+   toeplitz_gemm<<<grid, 128, smem, st>>>(mxh, mxl, mth, mtl, a.y, a.rows, a.n, a.k, a.err);
+   return cudaGetLastError();
+}
+
+}  // namespace risa_gb

@@ -128,9 +128,18 @@ cudaError_t launch_fan2para_adjoint(const float* par, float* fan, int batch, con
 struct FilterCfg {
    int rows, Dp, len;
    const float2* twiddle;  // [len] exp(-2 pi i k / len)
-   const float* h;         // [len/2 + 1]
+   const float2* h;        // [len] frequency response (Hermitian: the filter taps are real)
+   int adjoint;            // multiply by conj(h): the transposed filter
 };
 cudaError_t launch_filter(float* sino, int batch, const FilterCfg& cfg, cudaStream_t st);
+// Gradient of a loss with respect to the filter taps: the circular
+// cross-correlation of g (gradient at the filter output) with x (filter input)
+// summed over rows, at lag (j - center) mod len for tap j. workspace:
+// [blocks][len] float2 partial spectra.
+size_t filter_grad_workspace_bytes(const FilterCfg& cfg, int batch);
+cudaError_t launch_filter_taps_grad(const float* x, const float* g, int batch, const FilterCfg& cfg,
+                                    float2* workspace, int n_taps, int center, float* grad_taps,
+                                    cudaStream_t st);
 
 // ---------------------------------------------------------------- backprojection
 struct BPCfg {

@@ -154,4 +154,4 @@ def test_module_major_engine_matches_detector_major():
     dst = torch.empty_like(src)
     rg.reorder(src, dst, MODULES, 500, 432, n)
     torch.cuda.synchronize()
-    np.testing.assert_array_equal(dst.cpu().numpy().view(np.uint16), sc.raw)
+    np.testing.assert_array_equal(dst.cpu().numpy().view(np.uint16).reshape(sc.raw.shape), sc.raw)
