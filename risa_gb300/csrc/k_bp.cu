@@ -18,16 +18,16 @@ namespace risa_gb {
 
 namespace {
 
-// Linear interpolation variants: slices per CTA (S) and angles per chunk of
-// the pair kernel, plus the plain tile kernel. The nearest-neighbour modes
-// always use the plain tile kernel.
+// Linear interpolation variants: slices per CTA and angles per chunk of the
+// pair kernel, plus the plain tile kernel. The nearest-neighbour modes always
+// use the plain tile kernel.
 struct PairVariant {
    int slices, achunk;
    const char* name;
 };
 constexpr PairVariant kVariants[] = {
-    {2, 32, "pairs_s2_a32"}, {1, 32, "pairs_s1_a32"}, {4, 16, "pairs_s4_a16"},
-    {2, 16, "pairs_s2_a16"}, {4, 32, "pairs_s4_a32"}, {0, 32, "tile32_p4_a32"},
+    {2, 32, "pairs_s2_a32"}, {4, 16, "pairs_s4_a16"}, {4, 32, "pairs_s4_a32"},
+    {2, 16, "pairs_s2_a16"}, {1, 32, "pairs_s1_a32"}, {0, 32, "tile32_p4_a32"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -151,31 +151,30 @@ __global__ void __launch_bounds__(TX*(TY / PPT)) bp_tile(const float* __restrict
 // ---- linear interpolation, the hot kernel ---------------------------------------
 // A 32x32-pixel tile per CTA, 8 warps; each warp covers 8x4-pixel footprints
 // (so the bins one warp reads for an angle stay within ~16 consecutive
-// window entries, about two shared-memory wavefronts per 64-bit load) and
-// each thread 4 pixels spaced 8 rows apart. S slices of one geometry share a
-// CTA: the ray coordinate, bin index and weight of a pixel are computed once
-// and applied to every slice.
+// window entries) and each thread 4 pixels spaced 8 rows apart. S slices of
+// one geometry share a CTA: the ray coordinate, bin index and weight of a
+// pixel are computed once and applied to every slice.
 //
-// The window of an angle holds, for bin k, the pair (midpoint, difference) =
-// ((q[k] + q[k+1]) / 2, q[k+1] - q[k]), so the linearly interpolated value at
-// t = k + 1/2 + f (|f| <= 1/2) is mid + f * diff: one 64-bit shared load,
-// one add and one multiply-add per update. The bin index comes from the
-// round-to-nearest of t - 1/2 via the 1.5 * 2^23 magic constant, without
-// float/int conversion instructions.
+// The window of an angle holds, for bin k and slice s, the pair
+// (midpoint, difference) = ((q[k] + q[k+1]) / 2, q[k+1] - q[k]), so the
+// linearly interpolated value at t = k + 1/2 + f (|f| <= 1/2) is
+// mid + f * diff: one add and one multiply-add per update. The pairs of the S
+// slices of a bin are adjacent, so one 128-bit shared load serves two slices.
+// The bin index comes from the round-to-nearest of t - 1/2 via the
+// 1.5 * 2^23 magic constant, without float/int conversion instructions.
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
-constexpr size_t kMaxPairsSmem = 160 * 1024;
 constexpr int kMagicBits = 0x4B400000;
+constexpr size_t kMaxPairsSmem = 160 * 1024;
 
-template <int S>
+template <int S, int ACH>
 __global__ void __launch_bounds__(256) bp_linear_pairs(const float* __restrict__ sino,
                                                        float* __restrict__ img, BPCfg cfg, int wlen,
-                                                       int ACH, int batch) {
+                                                       int batch) {
    constexpr int T = 32, NT = 256;
-   extern __shared__ float2 wsm[];                          // [S][ACH][wlen]
-   float* s_a = reinterpret_cast<float*>(wsm + S * ACH * wlen);
-   float* s_b = s_a + ACH;
-   float* s_rel = s_b + ACH;
-   int* s_w0 = reinterpret_cast<int*>(s_rel + ACH);
+   extern __shared__ float4 wsm4[];  // [ACH][wlen][S] float2, 16-byte aligned
+   float2* wsm = reinterpret_cast<float2*>(wsm4);
+   __shared__ float s_a[ACH], s_b[ACH], s_rel[ACH];
+   __shared__ int s_w0[ACH];
 
    const int N = cfg.N, Dp = cfg.Dp, Pp = cfg.Pp;
    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
@@ -226,22 +225,32 @@ __global__ void __launch_bounds__(256) bp_linear_pairs(const float* __restrict__
          s_w0[threadIdx.x] = w0;
       }
       __syncthreads();
-      // one warp per (slice, angle) window, lanes along the bins: coalesced
-      // loads, no per-element division
-      for (int rowi = warp; rowi < S * na; rowi += NT / 32) {
-         const int si = rowi / na, ai = rowi - si * na;
+      // one warp per angle, lanes along the bins: coalesced loads per slice,
+      // the S pairs of a bin written next to each other
+      for (int ai = warp; ai < na; ai += NT / 32) {
          const int w0 = s_w0[ai];
-         float2* dst = wsm + (si * ACH + ai) * wlen;
-         const bool live = s0 + si < batch;
-         const float* row = sino + ((size_t)(s0 + si) * Pp + c0 + ai) * Dp;
+         float2* dst = wsm + (size_t)ai * wlen * S;
          for (int m = lane; m < wlen; m += 32) {
             const int k = w0 + m;
-            float q0 = 0.f, q1 = 0.f;
-            if (live) {
-               if (k >= 0 && k < Dp) q0 = __ldg(row + k);
-               if (k + 1 >= 0 && k + 1 < Dp) q1 = __ldg(row + k + 1);
+            float2 pr[S];
+#pragma unroll
+            for (int si = 0; si < S; ++si) {
+               float q0 = 0.f, q1 = 0.f;
+               if (s0 + si < batch) {
+                  const float* row = sino + ((size_t)(s0 + si) * Pp + c0 + ai) * Dp;
+                  if (k >= 0 && k < Dp) q0 = __ldg(row + k);
+                  if (k + 1 >= 0 && k + 1 < Dp) q1 = __ldg(row + k + 1);
+               }
+               pr[si] = make_float2(0.5f * (q0 + q1), q1 - q0);
             }
-            dst[m] = make_float2(0.5f * (q0 + q1), q1 - q0);
+            if (S == 1) {
+               dst[m] = pr[0];
+            } else {
+#pragma unroll
+               for (int h = 0; h < S / 2; ++h)
+                  reinterpret_cast<float4*>(dst + (size_t)m * S)[h] =
+                      make_float4(pr[2 * h].x, pr[2 * h].y, pr[2 * h + 1].x, pr[2 * h + 1].y);
+            }
          }
       }
       __syncthreads();
@@ -250,15 +259,23 @@ __global__ void __launch_bounds__(256) bp_linear_pairs(const float* __restrict__
          const float a = s_a[ai], b = s_b[ai];
          float tm = s_rel[ai] + (float)xo * a + (float)yo * b;
          const float step = 8.f * b;
+         const float2* wa = wsm + (size_t)ai * wlen * S;
 #pragma unroll
          for (int r = 0; r < 4; ++r) {
             const float v = tm + kMagic;
             const float f = tm - (v - kMagic);
             const unsigned k = min((unsigned)(__float_as_int(v) - kMagicBits), wmax);
+            if (S == 1) {
+               const float2 p = wa[k];
+               acc[0][r] = fmaf(f, p.y, acc[0][r] + p.x);
+            } else {
+               const float4* p4 = reinterpret_cast<const float4*>(wa + (size_t)k * S);
 #pragma unroll
-            for (int si = 0; si < S; ++si) {
-               const float2 p = wsm[(si * ACH + ai) * wlen + k];
-               acc[si][r] = fmaf(f, p.y, acc[si][r] + p.x);
+               for (int h = 0; h < S / 2; ++h) {
+                  const float4 p = p4[h];
+                  acc[2 * h][r] = fmaf(f, p.y, acc[2 * h][r] + p.x);
+                  acc[2 * h + 1][r] = fmaf(f, p.w, acc[2 * h + 1][r] + p.z);
+               }
             }
             tm += step;
          }
@@ -284,27 +301,37 @@ __global__ void __launch_bounds__(256) bp_linear_pairs(const float* __restrict__
    }
 }
 
-// Shared memory of one CTA: S windows of ach angles plus the per-angle scalars.
-inline size_t pairs_smem(int S, int ach, int wlen) {
-   return sizeof(float2) * (size_t)S * ach * wlen + sizeof(float) * 4 * ach;
-}
+// Dynamic shared memory of one CTA: the windows of ach angles for S slices.
+inline size_t pairs_smem(int S, int ach, int wlen) { return sizeof(float2) * (size_t)S * ach * wlen; }
 
-template <int S>
-cudaError_t launch_pairs(const float* sino, float* img, int batch, const BPCfg& cfg, int ach,
-                         cudaStream_t st) {
+template <int S, int ACH>
+cudaError_t launch_pairs(const float* sino, float* img, int batch, const BPCfg& cfg, cudaStream_t st) {
    const int wlen = window_len(cfg.scale, 32, 32);
-   // wide windows (many bins per pixel) get shorter angle chunks
-   while (ach > 4 && pairs_smem(S, ach, wlen) > kMaxPairsSmem) ach /= 2;
-   const size_t smem = pairs_smem(S, ach, wlen);
+   const size_t smem = pairs_smem(S, ACH, wlen);
    if (smem > kMaxPairsSmem) return cudaErrorInvalidConfiguration;
-   auto kern = bp_linear_pairs<S>;
+   auto kern = bp_linear_pairs<S, ACH>;
    if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
    }
    dim3 grid((cfg.N + 31) / 32, (cfg.N + 31) / 32, (batch + S - 1) / S);
-   kern<<<grid, 256, smem, st>>>(sino, img, cfg, wlen, ach, batch);
+   kern<<<grid, 256, smem, st>>>(sino, img, cfg, wlen, batch);
    return cudaGetLastError();
+}
+
+// Pair kernel with the variant's slices and angle chunk, halving the chunk
+// (down to 4 angles) while the windows of very wide tiles do not fit.
+template <int S>
+cudaError_t launch_pairs_fit(const float* sino, float* img, int batch, const BPCfg& cfg, int ach,
+                             cudaStream_t st) {
+   const int wlen = window_len(cfg.scale, 32, 32);
+   while (ach > 4 && pairs_smem(S, ach, wlen) > kMaxPairsSmem) ach /= 2;
+   switch (ach) {
+      case 32: return launch_pairs<S, 32>(sino, img, batch, cfg, st);
+      case 16: return launch_pairs<S, 16>(sino, img, batch, cfg, st);
+      case 8: return launch_pairs<S, 8>(sino, img, batch, cfg, st);
+      default: return launch_pairs<S, 4>(sino, img, batch, cfg, st);
+   }
 }
 
 template <int TX, int TY, int PPT, int ACH, int INTERP>
@@ -394,9 +421,9 @@ cudaError_t launch_backprojection(const float* sino, float* img, int batch, cons
       return launch_interp<32, 32, 4, 32>(sino, img, batch, cfg, st);
    const PairVariant& v = kVariants[variant];
    switch (v.slices) {
-      case 1: return launch_pairs<1>(sino, img, batch, cfg, v.achunk, st);
-      case 2: return launch_pairs<2>(sino, img, batch, cfg, v.achunk, st);
-      default: return launch_pairs<4>(sino, img, batch, cfg, v.achunk, st);
+      case 1: return launch_pairs_fit<1>(sino, img, batch, cfg, v.achunk, st);
+      case 2: return launch_pairs_fit<2>(sino, img, batch, cfg, v.achunk, st);
+      default: return launch_pairs_fit<4>(sino, img, batch, cfg, v.achunk, st);
    }
 }
 

@@ -137,9 +137,14 @@ def test_whole_map_adjoint():
     y = torch.from_numpy(rng.standard_normal((3, N, N)).astype(np.float32)).cuda()
     ax = FBPFunction.apply(x, h, g, p, 2)
     (aty,) = torch.autograd.grad(ax, x, grad_outputs=y)
-    lhs = float((ax.detach().double() * y.double()).sum())
-    rhs = float((x.detach().double() * aty.double()).sum())
-    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
+    # Dot-product test <Ax, y> == <x, A^T y>. Both sums cancel heavily (random
+    # signs), so the FP32 rounding of A x and A^T y is measured against the
+    # sum of the magnitudes of the terms, not against the cancelled total.
+    t_l = ax.detach().double() * y.double()
+    t_r = x.detach().double() * aty.double()
+    lhs, rhs = float(t_l.sum()), float(t_r.sum())
+    scale = max(float(t_l.abs().sum()), float(t_r.abs().sum()))
+    assert abs(lhs - rhs) <= 1e-5 * scale, (lhs, rhs, scale)
 
 
 def test_differentiation_configuration_fd_gradients():

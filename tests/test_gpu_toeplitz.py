@@ -1,0 +1,50 @@
+"""The filter as a split-bf16 Toeplitz GEMM on the tensor cores (tcgen05, TMEM
+accumulators, TMA-staged operands) against the FP64 oracle and the FFT path.
+
+Three bf16 terms with FP32 accumulation carry about 16-17 significant bits per
+product, so the bar here is max|err| / max|oracle| <= 1e-4 (the FFT path meets
+1e-5); the measured errors of both forms are reported by the benchmark's
+precision workload.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import risa_gb300 as rg
+from tests.helpers import rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _run(Pp, Dp, pad, ftype, batch, seed):
+    g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=64)
+    p = rg.make_params(filter_type=ftype, pad=pad)
+    tz = rg.Toeplitz(g, p)
+    fft = rg.Filter(g, p)
+    n, h = fft.response()
+    rng = np.random.default_rng(seed)
+    x = np.abs(rng.standard_normal((batch, Pp, Dp))).astype(np.float32)
+    t1 = torch.from_numpy(x).cuda()
+    t2 = t1.clone()
+    ws = torch.empty(tz.workspace_bytes(batch), dtype=torch.uint8, device="cuda")
+    tz.enqueue(t1, batch, ws)
+    fft.enqueue(t2, batch)
+    torch.cuda.synchronize()
+    tz.check()
+    got_t, got_f = t1.cpu().numpy(), t2.cpu().numpy()
+    ho = oracle.design_filter(n, rg.FILTERS[ftype], 1.0, oracle.QUIRK_NONE)
+    for b in range(min(batch, 2)):
+        exp = oracle.filter_rows(x[b], n, ho)
+        mt, _ = rel_err(got_t[b], exp)
+        mf, _ = rel_err(got_f[b], exp)
+        assert mf < 1e-5, mf
+        assert mt < 1e-4, mt
+
+
+def test_toeplitz_small_with_ragged_rows():
+    _run(Pp=100, Dp=128, pad=256, ftype="ramp", batch=3, seed=1)  # 300 rows: 3 tiles, last partial
+
+
+def test_toeplitz_precision_geometry():
+    _run(Pp=1024, Dp=1024, pad=2048, ftype="sheppLogan", batch=2, seed=2)
