@@ -154,6 +154,23 @@ size_t risa_gb_defects_workspace_bytes(const risa_gb_defects* h, int batch);
 risa_gb_status risa_gb_defects_enqueue(risa_gb_defects* h, uint16_t* frames, int batch,
                                        int32_t* flags_out, void* workspace, void* stream);
 risa_gb_status risa_gb_defects_destroy(risa_gb_defects* h);
+/* Allocation-free form of the two calls above; it has no counterpart in the
+ * reference. For callers that cannot allocate device memory once they are
+ * running -- a detector front-end that must not call the CUDA allocator during
+ * acquisition (allocation can synchronise the device and stall the frame
+ * stream), or a plug-in whose host framework owns all device memory and passes
+ * only input and output buffers. It creates no handle and takes no workspace:
+ * the scratch lives in a fixed 4 MiB device array inside the library, held on
+ * every GPU that loads it until the process exits. Batches whose scratch would
+ * exceed 4 MiB (about 180 frames of 1152 detectors per call) are rejected with
+ * RISA_GB_EINVAL. The first call on a device sets up that device (it looks up
+ * the array's address and uploads constants), so make it before any stream
+ * capture. All calls share the array and it keeps the last call's contents;
+ * calls whose GPU work overlaps race, so serialise them. Results are identical
+ * to risa_gb_defects_enqueue with the same geometry and params. */
+risa_gb_status risa_gb_defects_enqueue_noalloc(const risa_gb_geometry* g, const risa_gb_params* p,
+                                               uint16_t* frames, int batch, int32_t* flags_out,
+                                               void* stream);
 
 /* ---------------------------------------------------------------------------
  * Attenuation (Attenuation.cu:48-175, kernel :416-444). Create averages the

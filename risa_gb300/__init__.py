@@ -77,6 +77,7 @@ SIGNATURES = {
     "risa_gb_defects_workspace_bytes": (_sz, [_vp, _i]),
     "risa_gb_defects_enqueue": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
     "risa_gb_defects_destroy": (_i, [_vp]),
+    "risa_gb_defects_enqueue_noalloc": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "risa_gb_attenuation_create": (_i, [_vp, _vp, _vp, _i, _vp, _i, _pp]),
     "risa_gb_attenuation_enqueue": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
     "risa_gb_attenuation_tables": (_i, [_vp, _vp, _vp]),
