@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=64, help="frames per engine chunk (multiple of 2)")
     ap.add_argument("--distinct", type=int, default=8, help="distinct synthetic frames per plane")
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/roofline/cpu legs")
+    ap.add_argument("--bp-variant", type=int, default=-1,
+                    help="backprojection variant to use instead of autotuning (for profiling one kernel)")
     return ap.parse_args()
 
 
@@ -200,7 +202,11 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         fbp.enqueue(raw[:B], img[:B], rg.PLANES_INTERLEAVED, B, stream)
     stream.synchronize()
     bp = fbp.backprojection()
-    variant = bp.autotune(par_buf, img.data_ptr(), B, stream)
+    if args.bp_variant >= 0:
+        bp.set_variant(args.bp_variant)
+        variant = args.bp_variant
+    else:
+        variant = bp.autotune(par_buf, img.data_ptr(), B, stream)
     graph = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, stream)
     launches_per_step = graph.kernel_count
 

@@ -285,6 +285,17 @@ risa_gb_status risa_gb_backprojection_autotune(risa_gb_backprojection* h, const 
                                                int* variant_out);
 risa_gb_status risa_gb_backprojection_set_variant(risa_gb_backprojection* h, int variant);
 int risa_gb_backprojection_variant_count(void);
+/* Allocates the device buffer the asynchronous variants stage from (a padded
+ * (midpoint, difference) copy of the sinogram) for batches up to max_batch.
+ * Set-up call: may allocate and synchronise. Autotune and the FBP engine
+ * reserve for their batch themselves; an enqueue whose batch exceeds the
+ * reservation runs a variant that stages windows from the sinogram itself. */
+risa_gb_status risa_gb_backprojection_reserve(risa_gb_backprojection* h, int max_batch);
+/* Synchronises and returns RISA_GB_ETIMEDOUT if a bounded device-side wait of
+ * an earlier enqueue ran out (that tile's pixels were then not written). The
+ * asynchronous variants stage detector windows with bulk copies completed on
+ * mbarriers; their waits give up after a fixed number of polls. */
+risa_gb_status risa_gb_backprojection_check(risa_gb_backprojection* h);
 risa_gb_status risa_gb_backprojection_destroy(risa_gb_backprojection* h);
 
 /* ---------------------------------------------------------------------------

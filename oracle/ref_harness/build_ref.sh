@@ -3,6 +3,9 @@
 # in place, with outputs only under oracle/_ref/. Needs the reference checkout
 # (RISA_REF_ROOT, default /root/reference); prints a note and exits 0 without it.
 #   librisa_ref_host.so : the reference's host-side table builders (CPU only)
+#   risa_*.cubin        : the reference's stage kernels for sm_103a (device code
+#                         only; they travel to the GPU host, where
+#                         build_launch.sh builds the launcher that runs them)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${RISA_REF_ROOT:-/root/reference}"
@@ -26,3 +29,15 @@ done
 for p in "${pids[@]}"; do wait "$p"; done
 "$NVCC" -shared -o "$OUT/librisa_ref_host.so" "$OUT"/ref_host_*.o -lcufft -lgomp
 echo "build_ref: wrote $OUT/librisa_ref_host.so"
+# The reference's own stage kernels as device-only sm_103a cubins, compiled
+# in place from the stage sources with the reference's nvcc flags
+# (-O3 -use_fast_math); ref_launch.c loads and launches them on the GPU host.
+pids=()
+for stage in Attenuation Fan2Para Filter Backprojection Masking Reordering; do
+  lc="$(echo "$stage" | tr '[:upper:]' '[:lower:]')"
+  printf '#include "std_preinclude.h"\n#include "%s/%s.cu"\n' "$stage" "$stage" > "$OUT/risa_$lc.cu"
+  "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -O3 -use_fast_math -std=c++17 "${INC[@]}" \
+    -include "$HERE/stubs/risa_ref_preinclude.h" -w -o "$OUT/risa_$lc.cubin" "$OUT/risa_$lc.cu" & pids+=($!)
+done
+for p in "${pids[@]}"; do wait "$p"; done
+echo "build_ref: wrote $OUT/risa_*.cubin"

@@ -107,6 +107,8 @@ SIGNATURES = {
     "risa_gb_backprojection_autotune": (_i, [_vp, _vp, _vp, _i, _vp, ctypes.POINTER(ctypes.c_int)]),
     "risa_gb_backprojection_set_variant": (_i, [_vp, _i]),
     "risa_gb_backprojection_variant_count": (_i, []),
+    "risa_gb_backprojection_check": (_i, [_vp]),
+    "risa_gb_backprojection_reserve": (_i, [_vp, _i]),
     "risa_gb_backprojection_destroy": (_i, [_vp]),
     "risa_gb_masking_create": (_i, [_vp, _vp, _pp]),
     "risa_gb_masking_workspace_bytes": (_sz, [_vp, _i]),
@@ -437,6 +439,14 @@ class Backprojection(_Handle):
 
     def set_variant(self, v: int):
         _check(lib().risa_gb_backprojection_set_variant(self._h, v), "backprojection_set_variant")
+
+    def check(self):
+        """Synchronises; raises RisaError if a bounded device-side wait ran out."""
+        _check(lib().risa_gb_backprojection_check(self._h), "backprojection_check")
+
+    def reserve(self, max_batch: int):
+        """Device buffer for the staged variants at batches up to max_batch (set-up call)."""
+        _check(lib().risa_gb_backprojection_reserve(self._h, max_batch), "backprojection_reserve")
 
     @staticmethod
     def variant_count() -> int:

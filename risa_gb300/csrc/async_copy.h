@@ -1,0 +1,66 @@
+// Device helpers for asynchronous global->shared copies completed on
+// mbarriers (cp.async.bulk / cp.async.bulk.tensor), with bounded waits.
+//
+// Every wait here gives up after a fixed number of polls and reports it, so a
+// copy that never lands ends the kernel with an error code instead of a hang.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace risa_gb {
+namespace async {
+
+constexpr uint32_t kSpinLimit = 1u << 26;  // ~ seconds of polling
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+   return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Makes initialised mbarriers visible to the async proxy; follow with a CTA barrier.
+__device__ __forceinline__ void mbar_init_fence() {
+   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+   uint32_t ok;
+   asm volatile(
+       "{\n\t.reg .pred p;\n\t"
+       "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+       "selp.u32 %0, 1, 0, p;\n\t}"
+       : "=r"(ok)
+       : "r"(smem_u32(bar)), "r"(parity)
+       : "memory");
+   return ok != 0;
+}
+
+// Bounded wait; returns false (and records `code` in *err) when it gives up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+   for (uint32_t i = 0; i < kSpinLimit; ++i)
+      if (mbar_try_wait(bar, parity)) return true;
+   atomicCAS(err, 0, code);
+   return false;
+}
+
+// Contiguous global -> shared copy of `bytes` (multiple of 16; both addresses
+// 16-byte aligned) that completes `bytes` transactions on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+   asm volatile(
+       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+           smem_u32(dst)),
+       "l"(src), "r"(bytes), "r"(smem_u32(bar))
+       : "memory");
+}
+
+}  // namespace async
+}  // namespace risa_gb

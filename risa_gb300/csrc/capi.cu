@@ -245,6 +245,11 @@ struct risa_gb_backprojection {
    DevBuf a, b, ad, bd, t0;
    float norm = 0.f;
    int variant = 0;
+   // asynchronous variants: pair-sinogram padding without / with the fused
+   // mask's tile skipping, the pair buffer (grown outside stream capture) and
+   // the device error flag of their bounded waits
+   int win_lo[2] = {0, 0}, win_len[2] = {0, 0};
+   DevBuf pairs, err;
    BPCfg cfg(bool fused_mask) const {
       BPCfg c;
       c.Pp = g.Pp; c.Dp = g.Dp; c.N = g.N;
@@ -258,7 +263,26 @@ struct risa_gb_backprojection {
       // t' = t + shift; the texture variant truncates t + Dp/2
       const double shift = p.quirks == RISA_GB_QUIRKS_RISA ? (double)(int)(g.Dp * 0.5) : g.Dp * 0.5 - 0.5;
       c.trunc_offset = (float)(g.Dp * 0.5 - shift);
+      c.pairs = pairs.p;
+      c.pairs_bytes = pairs.bytes;
+      c.win_lo = win_lo[fused_mask ? 1 : 0];
+      c.win_len = win_len[fused_mask ? 1 : 0];
+      c.err = err.as<int>();
       return c;
+   }
+   // Pair buffer for `batch` slices under every variant. Only set-up calls
+   // (create of the engine, reserve, autotune) allocate; an enqueue whose
+   // batch exceeds the reservation runs a variant that needs no pair buffer.
+   risa_gb_status reserve(int batch) {
+      size_t need = 0;
+      for (int v = 0; v < bp_variant_count(); ++v)
+         need = std::max(need, bp_pairs_bytes(v, batch, g.Pp, std::max(win_len[0], win_len[1])));
+      if (need <= pairs.bytes) return RISA_GB_OK;
+      RG_CUDA(cudaDeviceSynchronize());
+      return pairs.alloc(need);
+   }
+   int variant_for(int batch, bool fused_mask) const {
+      return bp_pairs_bytes(variant, batch, g.Pp, win_len[fused_mask ? 1 : 0]) > pairs.bytes ? 0 : variant;
    }
 };
 
@@ -750,14 +774,26 @@ risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* gi, const r
    RG_TRY(h->ad.upload(t.ad));
    RG_TRY(h->bd.upload(t.bd));
    h->norm = t.norm;
+   const float scale = (float)((double)h->g.Dp / (double)h->g.N);
+   for (int m = 0; m < 2; ++m)
+      bp_window_extent(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(), t.t0.data(), h->g.Pp, h->g.N, scale,
+                       m == 1, &h->win_lo[m], &h->win_len[m]);
+   RG_TRY(h->err.alloc(sizeof(int)));
+   RG_CUDA(cudaMemset(h->err.p, 0, sizeof(int)));
    *out = h.release();
    return RISA_GB_OK;
 }
 
 static risa_gb_status bp_run(risa_gb_backprojection* h, const float* sino, float* img, int batch,
                              bool fused_mask, void* stream) {
-   RG_CUDA(launch_backprojection(sino, img, batch, h->cfg(fused_mask), h->variant, S(stream)));
+   RG_CUDA(launch_backprojection(sino, img, batch, h->cfg(fused_mask), h->variant_for(batch, fused_mask),
+                                 S(stream)));
    return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_backprojection_reserve(risa_gb_backprojection* h, int max_batch) {
+   if (!h || max_batch < 1) return fail(RISA_GB_EINVAL, "bad reserve arguments");
+   return h->reserve(max_batch);
 }
 
 risa_gb_status risa_gb_backprojection_enqueue(risa_gb_backprojection* h, const float* sino, float* img,
@@ -777,6 +813,17 @@ risa_gb_status risa_gb_backprojection_enqueue_adjoint(risa_gb_backprojection* h,
    return RISA_GB_OK;
 }
 
+risa_gb_status risa_gb_backprojection_check(risa_gb_backprojection* h) {
+   if (!h) return fail(RISA_GB_EINVAL, "null handle");
+   RG_CUDA(cudaDeviceSynchronize());
+   int code = 0;
+   RG_CUDA(cudaMemcpy(&code, h->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+   if (code)
+      return fail(RISA_GB_ETIMEDOUT, "backprojection: bounded wait ran out or window out of range (code " +
+                                         std::to_string(code) + ")");
+   return RISA_GB_OK;
+}
+
 int risa_gb_backprojection_variant_count(void) { return bp_variant_count(); }
 
 risa_gb_status risa_gb_backprojection_set_variant(risa_gb_backprojection* h, int variant) {
@@ -788,6 +835,7 @@ risa_gb_status risa_gb_backprojection_set_variant(risa_gb_backprojection* h, int
 risa_gb_status risa_gb_backprojection_autotune(risa_gb_backprojection* h, const float* sino, float* img,
                                                int batch, void* stream, int* variant_out) {
    if (!h || !sino || !img || batch < 1) return fail(RISA_GB_EINVAL, "bad autotune arguments");
+   RG_TRY(h->reserve(batch));  // every candidate then runs as itself
    cudaStream_t st = S(stream);
    cudaEvent_t e0, e1;
    RG_CUDA(cudaEventCreate(&e0));
@@ -797,7 +845,9 @@ risa_gb_status risa_gb_backprojection_autotune(risa_gb_backprojection* h, const 
    int best_v = 0;
    for (int v = 0; v < bp_variant_count(); ++v) {
       h->variant = v;
-      RG_TRY(bp_run(h, sino, img, batch, fused, stream));  // warm-up
+      // a variant whose staging does not fit this geometry is refused before
+      // launch (no sticky error); skip it
+      if (bp_run(h, sino, img, batch, fused, stream) != RISA_GB_OK) continue;  // warm-up
       RG_CUDA(cudaEventRecord(e0, st));
       for (int r = 0; r < 3; ++r) RG_TRY(bp_run(h, sino, img, batch, fused, stream));
       RG_CUDA(cudaEventRecord(e1, st));
@@ -810,7 +860,7 @@ risa_gb_status risa_gb_backprojection_autotune(risa_gb_backprojection* h, const 
    cudaEventDestroy(e1);
    h->variant = best_v;
    if (variant_out) *variant_out = best_v;
-   return RISA_GB_OK;
+   return risa_gb_backprojection_check(h);
 }
 
 risa_gb_status risa_gb_backprojection_destroy(risa_gb_backprojection* h) {
@@ -895,6 +945,7 @@ risa_gb_status risa_gb_fbp_create(const risa_gb_geometry* gi, const risa_gb_para
    RG_TRY(h->par.alloc(sizeof(float) * (size_t)max_batch * g.Pp * g.Dp));
    if (h->defects) RG_TRY(h->dws.alloc(risa_gb_defects_workspace_bytes(h->defects, max_batch)));
    RG_TRY(h->mm.alloc(sizeof(unsigned int) * 2 * (size_t)max_batch));
+   if (h->p.interp == RISA_GB_INTERP_LINEAR) RG_TRY(h->bp->reserve(max_batch));
    *out = h.release();
    return RISA_GB_OK;
 }

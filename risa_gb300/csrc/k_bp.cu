@@ -11,6 +11,10 @@
 // The ray coordinate of the tile origin is formed in FP64 per angle and the
 // per-pixel offset in FP32, which keeps the interpolation weight accurate to
 // ~1e-5 bins even for 1024+ bin detectors.
+#include <algorithm>
+#include <cmath>
+
+#include "async_copy.h"
 #include "kernels.h"
 #include "risa_gb300.h"
 
@@ -18,16 +22,21 @@ namespace risa_gb {
 
 namespace {
 
-// Linear interpolation variants: slices per CTA and angles per chunk of the
-// pair kernel, plus the plain tile kernel. The nearest-neighbour modes always
-// use the plain tile kernel.
-struct PairVariant {
-   int slices, achunk;
+// Linear interpolation variants: kernel kind, slices per CTA and angles per
+// chunk. The nearest-neighbour modes always use the plain tile kernel.
+enum VariantKind { kTile, kPairs, kAsync, kAsyncPacked };
+struct BPVariant {
+   int kind, slices, achunk;
    const char* name;
 };
-constexpr PairVariant kVariants[] = {
-    {2, 32, "pairs_s2_a32"}, {4, 16, "pairs_s4_a16"}, {4, 32, "pairs_s4_a32"},
-    {2, 16, "pairs_s2_a16"}, {1, 32, "pairs_s1_a32"}, {0, 32, "tile32_p4_a32"},
+constexpr BPVariant kVariants[] = {
+    {kPairs, 2, 32, "pairs_s2_a32"},         {kPairs, 4, 16, "pairs_s4_a16"},
+    {kPairs, 4, 32, "pairs_s4_a32"},         {kPairs, 2, 16, "pairs_s2_a16"},
+    {kPairs, 1, 32, "pairs_s1_a32"},         {kTile, 0, 32, "tile32_p4_a32"},
+    {kAsync, 2, 16, "async_s2_a16"},         {kAsync, 4, 8, "async_s4_a8"},
+    {kAsync, 4, 16, "async_s4_a16"},         {kAsyncPacked, 2, 16, "async_f32x2_s2_a16"},
+    {kAsyncPacked, 2, 32, "async_f32x2_s2_a32"}, {kAsyncPacked, 4, 8, "async_f32x2_s4_a8"},
+    {kAsyncPacked, 4, 16, "async_f32x2_s4_a16"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -334,6 +343,280 @@ cudaError_t launch_pairs_fit(const float* sino, float* img, int batch, const BPC
    }
 }
 
+// ---- linear interpolation with asynchronously staged windows -------------------
+// The arithmetic of bp_linear_pairs (the window origin formed with explicitly
+// rounded FP64 operations), split in two:
+//
+// bp_pairs_fill writes, once per slice group, the padded pair sinogram
+//    pairs[g][angle][u][S/2] float4, u = k + win_lo over k in [-win_lo, wp - win_lo),
+// where the float4 of slices (2h, 2h+1) of bin k is
+//    (mid_2h, mid_2h+1, diff_2h, diff_2h+1),  mid = (q[k] + q[k+1]) / 2, diff = q[k+1] - q[k],
+// with q = 0 outside the detector. The padding covers every window any tile
+// of the image can request, so a window is always one contiguous run of the
+// row and is fetched with a single bulk copy.
+//
+// bp_linear_async: warp 0 computes the window of each angle of a chunk and
+// issues one cp.async.bulk per angle into one of two shared-memory stages,
+// completing on that stage's mbarrier; all 8 warps backproject the other
+// stage meanwhile. One CTA barrier per chunk releases a stage for refill.
+// With PACKED the two slices of a float4 are accumulated with the paired
+// FP32 instructions add/fma.rn.f32x2 (one instruction for two updates, each
+// rounded like its scalar counterpart).
+//
+// Every mbarrier wait is bounded; on timeout the CTA records the error in
+// cfg.err, waits (bounded) for its own copies still in flight and returns
+// without writing its pixels.
+
+// Window start (bin of window entry 0) of tile origin (x0, y0) for angle
+// `ang`; the host mirrors this exactly to size the padding.
+__device__ __forceinline__ int tile_window_start(const BPCfg& cfg, int ang, int x0, int y0, float a, float b,
+                                                 double* base_out) {
+   const double base = __dadd_rn(__dadd_rn(__ldg(cfg.t0 + ang), __dmul_rn((double)x0, __ldg(cfg.ad + ang))),
+                                 __dmul_rn((double)y0, __ldg(cfg.bd + ang)));
+   const double tmin = __dadd_rn(__dadd_rn(base, (double)fminf(0.f, __fmul_rn(31.f, a))),
+                                 (double)fminf(0.f, __fmul_rn(31.f, b)));
+   *base_out = base;
+   return (int)floor(tmin) - 2;
+}
+
+template <int S>
+__global__ void __launch_bounds__(256) bp_pairs_fill(const float* __restrict__ sino, float4* __restrict__ pairs,
+                                                     int batch, int Pp, int Dp, int win_lo, int wp) {
+   const int u = blockIdx.x * 256 + threadIdx.x;
+   const int ang = blockIdx.y, g = blockIdx.z;
+   if (u >= wp) return;
+   const int k = u - win_lo;
+   float4* dst = pairs + (((size_t)g * Pp + ang) * wp + u) * (S / 2);
+#pragma unroll
+   for (int h = 0; h < S / 2; ++h) {
+      float q[2][2];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+         const int s = g * S + 2 * h + j;
+         const float* row = sino + ((size_t)s * Pp + ang) * Dp;
+         const bool live = s < batch;
+         q[j][0] = (live && k >= 0 && k < Dp) ? __ldg(row + k) : 0.f;
+         q[j][1] = (live && k + 1 >= 0 && k + 1 < Dp) ? __ldg(row + k + 1) : 0.f;
+      }
+      dst[h] = make_float4(0.5f * (q[0][0] + q[0][1]), 0.5f * (q[1][0] + q[1][1]), q[0][1] - q[0][0],
+                           q[1][1] - q[1][0]);
+   }
+}
+
+__device__ __forceinline__ unsigned long long f2_pack(float x, float y) {
+   unsigned long long r;
+   asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+   return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float& x, float& y) {
+   asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+   unsigned long long r;
+   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+   return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+   unsigned long long r;
+   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+   return r;
+}
+
+template <int S, int ACH, bool PACKED>
+__global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict__ pairs, float* __restrict__ img,
+                                                       BPCfg cfg, int wlen, int batch) {
+   constexpr int T = 32, H = S / 2;
+   extern __shared__ float4 wsm[];  // [2][ACH][wlen][H]
+   __shared__ uint64_t full[2];
+   __shared__ float s_a[2][ACH], s_b[2][ACH], s_rel[2][ACH];
+   __shared__ int s_fail;
+
+   const int N = cfg.N, Pp = cfg.Pp;
+   const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
+   const int g = blockIdx.z, s0 = g * S;
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int xo = (warp & 3) * 8 + (lane & 7);
+   const int yo = (warp >> 2) * 4 + (lane >> 3);
+   const float c = 0.5f * (float)(N - 1);
+   const float lim = (float)N * (float)N * 0.25f;
+
+   if (cfg.masking) {
+      const float nx = fminf(fmaxf(c, (float)x0), (float)(x0 + T - 1)) - c;
+      const float ny = fminf(fmaxf(c, (float)y0), (float)(y0 + T - 1)) - c;
+      if (nx * nx + ny * ny > lim) {
+         for (int si = 0; si < S; ++si) {
+            if (s0 + si >= batch) break;
+            float* out = img + (size_t)(s0 + si) * N * N;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+               const int x = x0 + xo, y = y0 + yo + 8 * r;
+               if (x < N && y < N) out[(size_t)y * N + x] = cfg.mask_value;
+            }
+         }
+         return;
+      }
+   }
+
+   const int nchunks = (Pp + ACH - 1) / ACH;
+   const size_t row_elems = (size_t)cfg.win_len * H;  // float4 per padded angle row
+   const float4* grow = pairs + (size_t)g * Pp * row_elems;
+   const uint32_t win_bytes = (uint32_t)(wlen * H * sizeof(float4));
+
+   // warp 0: parameters and bulk copies of chunk ch into stage st
+   auto issue = [&](int ch, int st) {
+      const int na = min(ACH, Pp - ch * ACH);
+      if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)na * win_bytes);
+      __syncwarp();
+      if (lane < na) {
+         const int ang = ch * ACH + lane;
+         const float a = __ldg(cfg.a + ang), b = __ldg(cfg.b + ang);
+         double base;
+         const int w0 = tile_window_start(cfg, ang, x0, y0, a, b, &base);
+         int u0 = w0 + cfg.win_lo;
+         if (u0 < 0 || u0 + wlen > cfg.win_len) {  // never with host-sized padding
+            atomicCAS(cfg.err, 0, 4);
+            u0 = min(max(u0, 0), cfg.win_len - wlen);
+         }
+         s_a[st][lane] = a;
+         s_b[st][lane] = b;
+         s_rel[st][lane] = (float)(base - (double)w0 - 0.5);
+         async::bulk_load(wsm + ((size_t)st * ACH + lane) * wlen * H, grow + (size_t)ang * row_elems + (size_t)u0 * H,
+                          win_bytes, &full[st]);
+      }
+   };
+
+   if (threadIdx.x == 0) {
+      async::mbar_init(&full[0], 1);
+      async::mbar_init(&full[1], 1);
+      s_fail = 0;
+      async::mbar_init_fence();
+   }
+   __syncthreads();
+   if (warp == 0) {
+      issue(0, 0);
+      if (nchunks > 1) issue(1, 1);
+   }
+   __syncthreads();
+
+   float acc[S][4];
+   unsigned long long acc2[H][4];
+#pragma unroll
+   for (int r = 0; r < 4; ++r) {
+#pragma unroll
+      for (int si = 0; si < S; ++si) acc[si][r] = 0.f;
+#pragma unroll
+      for (int h = 0; h < H; ++h) acc2[h][r] = 0ull;
+   }
+   const unsigned wmax = (unsigned)(wlen - 1);
+
+   for (int ch = 0; ch < nchunks; ++ch) {
+      const int st = ch & 1;
+      if (!async::mbar_wait(&full[st], (uint32_t)((ch >> 1) & 1), cfg.err, 5)) s_fail = 1;
+      const int na = min(ACH, Pp - ch * ACH);
+      const float4* wst = wsm + (size_t)st * ACH * wlen * H;
+#pragma unroll 2
+      for (int ai = 0; ai < na; ++ai) {
+         const float a = s_a[st][ai], b = s_b[st][ai];
+         float tm = s_rel[st][ai] + (float)xo * a + (float)yo * b;
+         const float step = 8.f * b;
+         const float4* wa = wst + (size_t)ai * wlen * H;
+#pragma unroll
+         for (int r = 0; r < 4; ++r) {
+            const float v = tm + kMagic;
+            const float f = tm - (v - kMagic);
+            const unsigned k = min((unsigned)(__float_as_int(v) - kMagicBits), wmax);
+            const float4* p4 = wa + (size_t)k * H;
+#pragma unroll
+            for (int h = 0; h < H; ++h) {
+               if (PACKED) {
+                  const ulonglong2 p = *reinterpret_cast<const ulonglong2*>(p4 + h);
+                  acc2[h][r] = f2_fma(f2_pack(f, f), p.y, f2_add(acc2[h][r], p.x));
+               } else {
+                  const float4 p = p4[h];
+                  acc[2 * h][r] = fmaf(f, p.z, acc[2 * h][r] + p.x);
+                  acc[2 * h + 1][r] = fmaf(f, p.w, acc[2 * h + 1][r] + p.y);
+               }
+            }
+            tm += step;
+         }
+      }
+      __syncthreads();
+      if (s_fail) {
+         // drain this CTA's copies still in flight, then leave without output
+         if (threadIdx.x == 0) {
+            int dummy = 0;
+            async::mbar_wait(&full[st], (uint32_t)((ch >> 1) & 1), &dummy, 1);
+            if (ch + 1 < nchunks) async::mbar_wait(&full[st ^ 1], (uint32_t)(((ch + 1) >> 1) & 1), &dummy, 1);
+         }
+         return;
+      }
+      if (warp == 0 && ch + 2 < nchunks) issue(ch + 2, st);
+   }
+   if (PACKED) {
+#pragma unroll
+      for (int h = 0; h < H; ++h)
+#pragma unroll
+         for (int r = 0; r < 4; ++r) f2_unpack(acc2[h][r], acc[2 * h][r], acc[2 * h + 1][r]);
+   }
+#pragma unroll
+   for (int si = 0; si < S; ++si) {
+      if (s0 + si >= batch) break;
+      float* out = img + (size_t)(s0 + si) * N * N;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+         const int x = x0 + xo, y = y0 + yo + 8 * r;
+         if (x < N && y < N) {
+            float v = acc[si][r] * cfg.norm;
+            if (cfg.masking) {
+               const float dx = (float)x - c, dy = (float)y - c;
+               if (dx * dx + dy * dy > lim) v = cfg.mask_value;
+            }
+            out[(size_t)y * N + x] = v;
+         }
+      }
+   }
+}
+
+inline size_t async_smem(int S, int ach, int wlen) { return 2 * sizeof(float2) * (size_t)S * ach * wlen; }
+
+template <int S, int ACH, bool PACKED>
+cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& cfg, cudaStream_t st) {
+   const int wlen = window_len(cfg.scale, 32, 32);
+   const size_t smem = async_smem(S, ACH, wlen);
+   if (smem > kMaxPairsSmem) return cudaErrorInvalidConfiguration;
+   // transaction bytes armed on one mbarrier phase stay below 2^20
+   if ((size_t)ACH * wlen * sizeof(float2) * S >= (1u << 20)) return cudaErrorInvalidConfiguration;
+   if (!cfg.pairs || !cfg.err || cfg.win_len < wlen) return cudaErrorInvalidValue;
+   const int groups = (batch + S - 1) / S;
+   if ((size_t)groups * S * cfg.Pp * cfg.win_len * sizeof(float2) > cfg.pairs_bytes) return cudaErrorInvalidValue;
+   bp_pairs_fill<S><<<dim3((cfg.win_len + 255) / 256, cfg.Pp, groups), 256, 0, st>>>(
+       sino, reinterpret_cast<float4*>(cfg.pairs), batch, cfg.Pp, cfg.Dp, cfg.win_lo, cfg.win_len);
+   cudaError_t e = cudaGetLastError();
+   if (e != cudaSuccess) return e;
+   auto kern = bp_linear_async<S, ACH, PACKED>;
+   if (smem > 48 * 1024) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+   }
+   dim3 grid((cfg.N + 31) / 32, (cfg.N + 31) / 32, groups);
+   kern<<<grid, 256, smem, st>>>(reinterpret_cast<const float4*>(cfg.pairs), img, cfg, wlen, batch);
+   return cudaGetLastError();
+}
+
+template <int S, bool PACKED>
+cudaError_t launch_async_fit(const float* sino, float* img, int batch, const BPCfg& cfg, int ach,
+                             cudaStream_t st) {
+   const int wlen = window_len(cfg.scale, 32, 32);
+   while (ach > 4 && async_smem(S, ach, wlen) > kMaxPairsSmem) ach /= 2;
+   switch (ach) {
+      case 32: return launch_async<S, 32, PACKED>(sino, img, batch, cfg, st);
+      case 16: return launch_async<S, 16, PACKED>(sino, img, batch, cfg, st);
+      case 8: return launch_async<S, 8, PACKED>(sino, img, batch, cfg, st);
+      default: return launch_async<S, 4, PACKED>(sino, img, batch, cfg, st);
+   }
+}
+
 template <int TX, int TY, int PPT, int ACH, int INTERP>
 cudaError_t launch_variant(const float* sino, float* img, int batch, const BPCfg& cfg,
                            cudaStream_t st) {
@@ -413,13 +696,61 @@ const char* bp_variant_name(int v) {
    return (v >= 0 && v < kNumVariants) ? kVariants[v].name : "invalid";
 }
 
+size_t bp_pairs_bytes(int variant, int batch, int Pp, int win_len) {
+   if (variant < 0 || variant >= kNumVariants || batch <= 0) return 0;
+   const BPVariant& v = kVariants[variant];
+   if (v.kind != kAsync && v.kind != kAsyncPacked) return 0;
+   const size_t groups = (size_t)(batch + v.slices - 1) / v.slices;
+   return groups * v.slices * (size_t)Pp * (size_t)win_len * sizeof(float2);
+}
+
+void bp_window_extent(const float* a, const float* b, const double* ad, const double* bd, const double* t0,
+                      int Pp, int N, float scale, bool masking, int* win_lo, int* win_len) {
+   // mirrors tile_window_start and the tile skip test of bp_linear_async
+   // (host code is compiled without floating-point contraction)
+   const int wlen = window_len(scale, 32, 32);
+   const int tiles = (N + 31) / 32;
+   const double c = 0.5 * (double)(N - 1), lim = (double)N * (double)N * 0.25;
+   long lo = 0x7fffffff, hi = -0x7fffffff;
+   for (int by = 0; by < tiles; ++by) {
+      for (int bx = 0; bx < tiles; ++bx) {
+         const int x0 = bx * 32, y0 = by * 32;
+         if (masking) {
+            const double nx = std::fmin(std::fmax(c, (double)x0), (double)(x0 + 31)) - c;
+            const double ny = std::fmin(std::fmax(c, (double)y0), (double)(y0 + 31)) - c;
+            if (nx * nx + ny * ny > lim * (1.0 + 1e-6) + 1.0) continue;  // surely skipped
+         }
+         for (int i = 0; i < Pp; ++i) {
+            const double base = (t0[i] + (double)x0 * ad[i]) + (double)y0 * bd[i];
+            const float ma = 31.f * a[i], mb = 31.f * b[i];
+            const double tmin = (base + (double)std::fmin(0.f, ma)) + (double)std::fmin(0.f, mb);
+            const long w0 = (long)std::floor(tmin) - 2;
+            lo = std::min(lo, w0);
+            hi = std::max(hi, w0 + wlen);
+         }
+      }
+   }
+   if (lo > hi) lo = hi = 0;
+   // two bins of slack either side; k = u - win_lo
+   *win_lo = (int)(2 - lo);
+   *win_len = (int)(hi - lo + 4);
+}
+
 cudaError_t launch_backprojection(const float* sino, float* img, int batch, const BPCfg& cfg,
                                   int variant, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
    if (cfg.interp != RISA_GB_INTERP_LINEAR || variant < 0 || variant >= kNumVariants ||
-       kVariants[variant].slices == 0)
+       kVariants[variant].kind == kTile)
       return launch_interp<32, 32, 4, 32>(sino, img, batch, cfg, st);
-   const PairVariant& v = kVariants[variant];
+   const BPVariant& v = kVariants[variant];
+   if (v.kind == kAsync) {
+      if (v.slices == 2) return launch_async_fit<2, false>(sino, img, batch, cfg, v.achunk, st);
+      return launch_async_fit<4, false>(sino, img, batch, cfg, v.achunk, st);
+   }
+   if (v.kind == kAsyncPacked) {
+      if (v.slices == 2) return launch_async_fit<2, true>(sino, img, batch, cfg, v.achunk, st);
+      return launch_async_fit<4, true>(sino, img, batch, cfg, v.achunk, st);
+   }
    switch (v.slices) {
       case 1: return launch_pairs_fit<1>(sino, img, batch, cfg, v.achunk, st);
       case 2: return launch_pairs_fit<2>(sino, img, batch, cfg, v.achunk, st);

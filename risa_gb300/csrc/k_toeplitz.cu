@@ -29,50 +29,23 @@
 
 #include <cstdint>
 
+#include "async_copy.h"
 #include "kernels.h"
 #include "toeplitz.h"
 
 namespace risa_gb {
 
 namespace {
+using async::mbar_arrive_expect_tx;
+using async::mbar_init;
+using async::mbar_try_wait;
+using async::mbar_wait;
+using async::smem_u32;
+
 constexpr int kBM = 128, kBN = 128, kBK = 64, kStages = 3;
 constexpr int kTileBytes = kBM * kBK * 2;                  // 16 KiB per operand tile
 constexpr int kStageBytes = 4 * kTileBytes;                // Xh, Xl, Th, Tl
-constexpr uint32_t kSpinLimit = 1u << 26;                  // ~ seconds of polling
 constexpr uint32_t kTmemCols = 128;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-   return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-   uint32_t ok;
-   asm volatile(
-       "{\n\t.reg .pred p;\n\t"
-       "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-       "selp.u32 %0, 1, 0, p;\n\t}"
-       : "=r"(ok)
-       : "r"(smem_u32(bar)), "r"(parity)
-       : "memory");
-   return ok != 0;
-}
-
-// Bounded wait; returns false (and records the error) when it gives up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
-   for (uint32_t i = 0; i < kSpinLimit; ++i)
-      if (mbar_try_wait(bar, parity)) return true;
-   atomicCAS(err, 0, code);
-   return false;
-}
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
    asm volatile(

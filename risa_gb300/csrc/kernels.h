@@ -155,9 +155,22 @@ struct BPCfg {
    int interp;          // RISA_GB_INTERP_*
    float scale;         // Dp / N (bins per pixel)
    float trunc_offset;  // texture variant truncates t' + trunc_offset (= t + Dp/2)
+   // asynchronous variants: padded pair sinogram (bins k in [-win_lo, win_len - win_lo))
+   void* pairs = nullptr;
+   size_t pairs_bytes = 0;
+   int win_lo = 0, win_len = 0;
+   int* err = nullptr;  // device flag: nonzero after a bounded wait gave up
 };
 int bp_variant_count();
 const char* bp_variant_name(int v);
+// Device bytes of the pair sinogram that `variant` needs for `batch` slices
+// (0 for variants that stage windows from the sinogram itself).
+size_t bp_pairs_bytes(int variant, int batch, int Pp, int win_len);
+// Padding of the pair sinogram: the bin range covering every window that a
+// 32 x 32 tile of the image requests (only tiles meeting the inscribed circle
+// when `masking`), computed with the kernel's own arithmetic.
+void bp_window_extent(const float* a, const float* b, const double* ad, const double* bd, const double* t0,
+                      int Pp, int N, float scale, bool masking, int* win_lo, int* win_len);
 cudaError_t launch_backprojection(const float* sino, float* img, int batch, const BPCfg& cfg,
                                   int variant, cudaStream_t st);
 cudaError_t launch_backprojection_adjoint(const float* img, float* sino, int batch,

@@ -178,6 +178,7 @@ def test_backprojection(quirk, interp):
     g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=N, rotation_offset=-7.5)
     p = rg.make_params(quirks=quirk, interp=interp)
     bp = rg.Backprojection(g, p)
+    bp.reserve(4)  # pair buffer, so the staged variants run as themselves
     sino, _ = phantom.parallel_sinograms(2, Pp, Dp, 200.0, seed=4)
     img = torch.empty((2, N, N), dtype=torch.float32, device="cuda")
     for v in range(rg.Backprojection.variant_count()):
@@ -189,6 +190,7 @@ def test_backprojection(quirk, interp):
             mr, _ = rel_err(got[b], exp)
             tol = MAX_REL if interp == rg.INTERP_LINEAR else 2e-3  # nearest: exact .5 ties may round apart
             assert mr < tol, (v, b, mr)
+    bp.check()
 
 
 def test_backprojection_masking_and_autotune():
@@ -196,18 +198,25 @@ def test_backprojection_masking_and_autotune():
     g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=N)
     p = rg.make_params(masking=True, masking_value=-1.0)
     bp = rg.Backprojection(g, p)
+    bp.reserve(4)  # pair buffer, so the staged variants run as themselves
     sino, _ = phantom.parallel_sinograms(3, Pp, Dp, 200.0, seed=9)
     img = torch.empty((3, N, N), dtype=torch.float32, device="cuda")
-    v = bp.autotune(dev(sino), img, 3)
-    assert 0 <= v < rg.Backprojection.variant_count()
-    bp.enqueue(dev(sino), img, 3)
-    got = host(img)
-    for b in range(3):
-        exp = oracle.mask(oracle.backproject(sino[b], N), -1.0)
-        assert rel_err(got[b], exp)[0] < MAX_REL
-        yy, xx = np.mgrid[:N, :N]
-        out = (xx - (N - 1) / 2) ** 2 + (yy - (N - 1) / 2) ** 2 > N * N / 4
-        assert np.all(got[b][out] == -1.0)
+    exps = [oracle.mask(oracle.backproject(sino[b], N), -1.0) for b in range(3)]
+    yy, xx = np.mgrid[:N, :N]
+    out = (xx - (N - 1) / 2) ** 2 + (yy - (N - 1) / 2) ** 2 > N * N / 4
+    # every variant with the fused mask (tiles outside the circle skipped)
+    for v in list(range(rg.Backprojection.variant_count())) + ["autotuned"]:
+        if v == "autotuned":
+            assert 0 <= bp.autotune(dev(sino), img, 3) < rg.Backprojection.variant_count()
+        else:
+            bp.set_variant(v)
+        img.fill_(np.nan)
+        bp.enqueue(dev(sino), img, 3)
+        got = host(img)
+        bp.check()
+        for b in range(3):
+            assert rel_err(got[b], exps[b])[0] < MAX_REL, (v, b)
+            assert np.all(got[b][out] == -1.0), (v, b)
 
 
 def test_masking_normalisation():

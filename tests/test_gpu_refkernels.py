@@ -1,0 +1,245 @@
+"""GPU parity against the reference's OWN kernels.
+
+The reference's stage kernels (compiled from its sources to sm_103a cubins by
+oracle/ref_harness/build_ref.sh and launched by oracle/ref_harness/ref_launch.c
+exactly as its processor() loops launch them) and this library's kernels run
+on the same device buffers; the library runs in RISA mode, which reproduces
+the reference's index conventions. The reference is built with
+-use_fast_math, so its FP32 results differ from IEEE-rounded ones in the last
+bits: FP32 outputs are compared with max|lib - ref| / max|ref| <= 1e-5,
+integer outputs bit for bit. Inputs of the reference kernels are checked on
+the CPU first (grid coverage, table indices in range), since some of them
+index without bounds checks.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import risa_gb300 as rg
+from risa_gb300 import phantom
+from tests.helpers import SMALL, geom, ns, rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import ref_kernels as rk  # noqa: E402
+
+MAX_REL = 1e-5
+BLOCK = 16  # blockSize2D of the reference's example configuration
+
+ROFEX_F2P = dict(n_planes=2, n_fan_det=432, n_fan_proj=500, n_par_proj=32, n_par_det=48,
+                 source_offset=23.2, detector_diameter=216.0, image_center_x=0.0, image_center_y=0.0,
+                 image_width=190.0, source_diameter=[365.0, 370.0], delta_x=[815.0, 815.0],
+                 delta_z=[1417.0, 1430.0], source_angle=[240.0, 240.0])
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _ref():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    why = rk.unavailable()
+    if why:
+        pytest.skip(why)
+    torch.cuda.init()
+    torch.zeros(1, device="cuda")  # makes the primary context current for the driver API
+    rk.lib()
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+# ------------------------------------------------------------------------------ attenuation
+@pytest.mark.parametrize("relevant", [False, True])
+def test_attenuation_vs_reference_kernel(relevant):
+    d = dict(SMALL, n_planes=2, source_diameter=[430.0, 430.0], delta_x=[0, 0], delta_z=[1417, 1430],
+             source_angle=[360, 360], source_offset=23.2)
+    P, D = d["n_fan_proj"], d["n_fan_det"]
+    sc = phantom.make_scan(4, 2, P, D, 215.0, 240.0, seed=11, defect_fraction=0.0, distinct=4)
+    fix = (43, 285, 175, 362, 0, 431)
+    p = rg.make_params(quirks=rg.QUIRKS_RISA, relevant_mask=relevant, lower_lim_offset=47.0,
+                       upper_lim_offset=313.0, fix_points=fix)
+    att = rg.Attenuation(geom(d), p, sc.ref, 1, sc.dark, 1)
+    ref_avg, dark_avg = att.tables()
+    if relevant:
+        m = oracle.relevant_area_mask(D, P, 23.2, 47.0, 313.0, *fix).astype(np.float32)
+    else:
+        m = np.ones((P, D), np.float32)
+    raw = sc.raw  # [4][P][D], planes interleaved
+    out = torch.empty(raw.shape, dtype=torch.float32, device="cuda")
+    att.enqueue(dev(raw.view(np.int16)), out, rg.PLANES_INTERLEAVED, raw.shape[0])
+    got = host(out)
+    t_ref, t_dark, t_mask = dev(ref_avg), dev(dark_avg), dev(m)
+    ref_out = torch.empty((P, D), dtype=torch.float32, device="cuda")
+    for b in range(raw.shape[0]):
+        rk.attenuation(dev(raw[b].view(np.int16)), t_mask, ref_out, t_ref, t_dark, D, P, b % 2, BLOCK)
+        exp = host(ref_out)
+        mr, _ = rel_err(got[b], exp)
+        assert mr < MAX_REL, (b, mr)
+        np.testing.assert_array_equal(got[b][m == 0], exp[m == 0])
+
+
+# ------------------------------------------------------------------------------ fan2para
+def test_fan2para_vs_reference_kernel(golden_dir):
+    gd = ROFEX_F2P
+    L, Pf, Df, Pp, Dp = gd["n_planes"], gd["n_fan_proj"], gd["n_fan_det"], gd["n_par_proj"], gd["n_par_det"]
+    Pp2 = 2 * Pp
+    z = np.load(os.path.join(golden_dir, "f2p_rofex.npz"))
+    itab, ftab = z["itab"], z["ftab"]
+    # the reference kernel's bounds test lets threads past the detector edge run
+    # unless the grid covers the sinogram exactly; its table reads are unchecked
+    assert Dp % BLOCK == 0 and Pp2 % BLOCK == 0
+    for r in (0, 1):
+        on = itab[8 + r] != 0
+        for row, lim in ((0 + r, Pf), (2 + r, Pf), (4 + r, Df), (6 + r, Df)):
+            v = itab[row][on]
+            assert v.min() >= 0 and v.max() < lim
+    order = [itab[0], itab[1], itab[2], itab[3], itab[6], itab[7], itab[4], itab[5],
+             ftab[0], ftab[1], ftab[2], ftab[3], itab[8], itab[9]]
+    tables = [dev(t) for t in order]
+    params = np.zeros(11, np.int32)
+    params[:5] = (L, Df, Pf, Pp2, Dp)
+    params[5:].view(np.float32)[:] = (gd["source_offset"], gd["detector_diameter"],
+                                      gd["detector_diameter"] / 2.0, gd["image_center_x"],
+                                      gd["image_center_y"], gd["image_width"])
+    t_params = dev(params)
+    f2p = rg.Fan2Para(geom(gd), rg.make_params(quirks=rg.QUIRKS_RISA))
+    rec = oracle.f2p_records(ns(gd), oracle.QUIRK_RISA)
+    rng = np.random.default_rng(7)
+    fan = rng.standard_normal((L, Pf, Df)).astype(np.float32)
+    par = torch.empty((1, Pp, Dp), dtype=torch.float32, device="cuda")
+    t_g, t_t, t_a, t_s = dev(z["gamma"]), dev(z["theta"]), dev(z["alpha"]), dev(z["s"])
+    for k in range(L):
+        f2p.enqueue(dev(fan[k:k + 1]), par, k, 1)
+        got = host(par)[0]
+        ref_par = torch.zeros(Pp2 * Dp, dtype=torch.float32, device="cuda")
+        rk.fan2para(k, dev(fan[k]), ref_par, t_g, t_t, t_a, t_s, tables, t_params, Dp, Pp2, BLOCK)
+        exp = host(ref_par)[:Pp * Dp].reshape(Pp, Dp)
+        # The reference forms its interpolation weights with -use_fast_math
+        # divisions (2 ulp), which moves its own output up to ~1e-5 (of the
+        # maximum) away from the FP64 result; the library meets 1e-5 against
+        # FP64 and 2e-5 against the reference kernel.
+        exact = oracle.f2p_apply(rec, k, oracle.QUIRK_RISA, fan[k])
+        e_lib, e_ref, e_pair = rel_err(got, exact)[0], rel_err(exp, exact)[0], rel_err(got, exp)[0]
+        print(f"plane {k}: lib vs FP64 {e_lib:.2e}, reference kernel vs FP64 {e_ref:.2e}, lib vs reference {e_pair:.2e}")
+        assert e_lib < MAX_REL, (k, e_lib)
+        assert e_pair < 2 * MAX_REL, (k, e_pair, e_ref)
+
+
+# ------------------------------------------------------------------------------ filter
+@pytest.mark.parametrize("dp,ftype", [(256, "ramp"), (256, "sheppLogan"), (1024, "hamming"),
+                                      (2048, "cosine"), (1024, "hanning")])
+def test_filter_vs_reference_cufft_path(golden_dir, dp, ftype):
+    rows = 48
+    g = rg.make_geometry(n_par_proj=rows, n_par_det=dp, n_pixels=64)
+    p = rg.make_params(quirks=rg.QUIRKS_RISA, filter_type=ftype)
+    filt = rg.Filter(g, p)
+    n, h = filt.response()
+    hf = np.load(os.path.join(golden_dir, "filters.npz"))[f"h_{dp}_{rg.FILTERS[ftype]}_1.0"]
+    assert n == dp
+    np.testing.assert_array_equal(np.asarray(h, np.float32).view(np.uint32), hf.view(np.uint32))
+    rng = np.random.default_rng(dp)
+    x = np.abs(rng.standard_normal((rows, dp))).astype(np.float32)
+    t = dev(x[None])
+    filt.enqueue(t, 1)
+    got = host(t)[0]
+    ts = dev(x)
+    freq = torch.empty((rows, dp // 2 + 1, 2), dtype=torch.float32, device="cuda")
+    rk.filter_rows(ts, freq, dev(hf), dp, rows, BLOCK)
+    exp = host(ts)
+    mr, _ = rel_err(got, exp)
+    assert mr < MAX_REL, mr
+
+
+# ------------------------------------------------------------------------------ backprojection
+def _bp_constants(Pp, Dp, N, rot):
+    """The host set-up of Backprojection::processor (Backprojection.cu:118-138)."""
+    sin_t = np.zeros(Pp, np.float32)
+    cos_t = np.zeros(Pp, np.float32)
+    for i in range(Pp):
+        th = np.float32(i * np.pi / float(np.float32(Pp)) + float(np.float32(rot)) / 180.0 * np.pi)
+        while th < 0.0:
+            th = np.float32(float(th) + 2.0 * np.pi)
+        sin_t[i] = np.float32(np.sin(np.float64(th)))
+        cos_t[i] = np.float32(np.cos(np.float64(th)))
+    scale = np.float32(Dp / float(np.float32(N)))
+    norm = np.float32(np.pi / Pp / float(scale))
+    center = np.float32((N - 1.0) * 0.5)
+    return sin_t, cos_t, float(norm), float(scale), float(center)
+
+
+@pytest.mark.parametrize("interp", [rg.INTERP_LINEAR, rg.INTERP_NEAREST])
+@pytest.mark.parametrize("Pp,Dp,N,rot", [(256, 256, 192, -7.5), (360, 512, 256, 0.0), (1024, 1024, 512, 0.0)])
+def test_backprojection_vs_reference_kernel(interp, Pp, Dp, N, rot):
+    g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=N, rotation_offset=rot)
+    p = rg.make_params(quirks=rg.QUIRKS_RISA, interp=interp)
+    bp = rg.Backprojection(g, p)
+    bp.reserve(4)  # pair buffer, so the staged variants run as themselves
+    sino, _ = phantom.parallel_sinograms(2, Pp, Dp, 200.0, seed=Pp)
+    sin_t, cos_t, norm, scale, center = _bp_constants(Pp, Dp, N, rot)
+    rk.bp_constants(sin_t, cos_t, Pp, norm, scale, center)
+    img = torch.empty((2, N, N), dtype=torch.float32, device="cuda")
+    ref_img = torch.empty((N, N), dtype=torch.float32, device="cuda")
+    nvar = rg.Backprojection.variant_count() if interp == rg.INTERP_LINEAR else 1
+    for v in range(nvar):
+        bp.set_variant(v)
+        bp.enqueue(dev(sino), img, 2)
+        got = host(img)
+        for b in range(2):
+            rk.backproject(interp == rg.INTERP_NEAREST, dev(sino[b]), ref_img, N, Pp, Dp, BLOCK)
+            exp = host(ref_img)
+            mr, _ = rel_err(got[b], exp)
+            if interp == rg.INTERP_LINEAR:
+                assert mr < MAX_REL, (v, b, mr)
+            else:
+                # nearest: a ray coordinate within an ulp of a .5 tie may round to
+                # the other bin under the reference's fast-math arithmetic
+                assert mr < 2e-3, (b, mr)
+                assert np.mean(np.abs(got[b] - exp) <= MAX_REL * np.abs(exp).max()) > 0.999
+
+
+# ------------------------------------------------------------------------------ masking
+@pytest.mark.parametrize("N", [200, 512])
+def test_masking_vs_reference_kernel(N):
+    g = rg.make_geometry(n_par_proj=64, n_par_det=64, n_pixels=N)
+    p = rg.make_params(quirks=rg.QUIRKS_RISA, masking=True, masking_value=-3.0)
+    m = rg.Masking(g, p)
+    rng = np.random.default_rng(N)
+    x = rng.standard_normal((1, N, N)).astype(np.float32)
+    t = dev(x)
+    ws = torch.empty(max(m.workspace_bytes(1), 1), dtype=torch.uint8, device="cuda")
+    m.enqueue(t, 1, ws)
+    got = host(t)[0]
+    tr = dev(x[0])
+    rk.mask(tr, -3.0, N)
+    np.testing.assert_array_equal(got.view(np.uint32), host(tr).view(np.uint32))
+
+
+# ------------------------------------------------------------------------------ reordering
+def test_reordering_vs_reference_kernel():
+    modules, per, P = 27, 16, 500
+    D = modules * per
+    # Reordering::createHashTable (Reordering.cu:180-193)
+    table = np.empty(P * D, np.int32)
+    i = 0
+    for proj in range(P):
+        for mod in range(modules):
+            table[i:i + per] = np.arange(per) + proj * per + mod * per * P
+            i += per
+    assert table.min() >= 0 and table.max() < P * D
+    rng = np.random.default_rng(3)
+    raw = rng.integers(0, 65536, size=(2, P * D), dtype=np.uint16)
+    out = torch.empty((2, P, D), dtype=torch.int16, device="cuda")
+    rg.reorder(dev(raw.view(np.int16)), out, modules, P, D, 2)
+    got = host(out).view(np.uint16)
+    ref_out = torch.empty((P, D), dtype=torch.int16, device="cuda")
+    for b in range(2):
+        rk.reorder(dev(raw[b].view(np.int16)), ref_out, dev(table), P, D)
+        np.testing.assert_array_equal(got[b], host(ref_out).view(np.uint16))
