@@ -39,6 +39,11 @@ WORKLOAD = dict(n_planes=2, n_fan_det=1152, n_fan_proj=1000, n_par_proj=1024, n_
                 delta_x=[0.0, 0.0], delta_z=[1417.0, 1430.0], source_angle=[360.0, 360.0])
 FRAMES_PER_PLANE = 2000
 FLOPS_PER_UPDATE = 6  # ray coordinate FMA (2) + weight add (1) + interpolation FMA (2) + accumulate (1)
+SMEM_BYTES_PER_UPDATE = 8  # one FP32 (midpoint, difference) pair per pixel x angle and slice
+SMEM_BYTES_PER_CLK_SM = 128  # nominal shared-memory bandwidth per SM
+# dram__bytes_read.sum + dram__bytes_write.sum of one 64-slice backprojection launch
+# (profiles/bp_staged_fbp512_ncu.txt)
+BP_DRAM_BYTES_PER_LAUNCH = 671.0e6
 WORKLOAD_NAME = ("full-rate streaming: 2 planes x 2000 frames of 1000x1152 uint16 fan sinograms, 1% defective "
                  "detectors -> 1024x1024 parallel (pad 2048, Shepp-Logan) -> 512^2 FP32, circular mask")
 
@@ -305,6 +310,7 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     par_copy = torch.randn((B, Pp, Dp), dtype=torch.float32, device=dev)
     t_filt = timed(torch, stream, lambda: filt.enqueue(par_copy, B, stream), reps)
     t_bp = timed(torch, stream, lambda: bp.enqueue(par_buf, img[:B], B, stream), reps)
+    t_stage, t_kern = bp.time(par_buf, img[:B], B, reps, stream)
     dfx_b = rg.Defects(g, p, max_batch=B)
     ws_b = torch.empty(dfx_b.workspace_bytes(B), dtype=torch.uint8, device=dev)
     raw_b = raw[:B].clone()
@@ -316,18 +322,28 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     yy, xx = np.mgrid[:N, :N]
     inside = int(((xx - (N - 1) / 2) ** 2 + (yy - (N - 1) / 2) ** 2 <= N * N / 4).sum())
     updates = B * inside * Pp
-    bp_tflops = updates * FLOPS_PER_UPDATE / (t_bp / 1e3) / 1e12
+    # The backprojection kernel is bound by shared-memory bandwidth: every
+    # update reads one FP32 (midpoint, difference) pair of its slice (8 B).
+    smem_peak = SMEM_BYTES_PER_CLK_SM * sms * sm_mhz * 1e6 / 1e9  # GB/s
+    smem_gbs = updates * SMEM_BYTES_PER_UPDATE / (t_kern / 1e3) / 1e9
+    bp_tflops = updates * FLOPS_PER_UPDATE / (t_kern / 1e3) / 1e12
     out["roofline"] = {
-        "kernel": "bp_tile (backprojection)", "bound": "fp32", "achieved": bp_tflops, "peak": fp32_peak,
-        "unit": "TFLOP/s", "frac": bp_tflops / fp32_peak, "traffic": None,
-        "work": f"{FLOPS_PER_UPDATE} FLOP per pixel x angle update, {inside} in-circle pixels x {Pp} angles "
-                f"x {B} slices per launch",
-        "peak_source": f"nominal FFMA rate: 128 lanes x 2 FLOP x {sms} SMs x {sm_mhz:.0f} MHz "
-                       "(MEASURED_PEAKS.json carries no FP32 figure)",
+        "kernel": f"bp_linear_async ({rg.Backprojection.variant_name(variant)})", "bound": "smem",
+        "achieved": smem_gbs, "peak": smem_peak, "unit": "GB/s", "frac": smem_gbs / smem_peak,
+        "traffic": BP_DRAM_BYTES_PER_LAUNCH,
+        "work": f"{SMEM_BYTES_PER_UPDATE} B of shared-memory reads per pixel x angle update and slice, "
+                f"{inside} in-circle pixels x {Pp} angles x {B} slices per launch",
+        "peak_source": f"nominal shared-memory bandwidth {SMEM_BYTES_PER_CLK_SM} B/clk/SM x {sms} SMs x "
+                       f"{sm_mhz:.0f} MHz (MEASURED_PEAKS.json carries no shared-memory figure)",
+        "kernel_ms": t_kern, "staging_ms": t_stage,
+        "fp32": {"achieved": bp_tflops, "peak": fp32_peak, "unit": "TFLOP/s", "frac": bp_tflops / fp32_peak,
+                 "work": f"{FLOPS_PER_UPDATE} FLOP per update",
+                 "peak_source": f"nominal FFMA rate 128 lanes x 2 FLOP x {sms} SMs x {sm_mhz:.0f} MHz"},
     }
     out["bp"] = {"gupdates_per_s": updates / (t_bp / 1e3) / 1e9,
+                 "gupdates_per_s_kernel": updates / (t_kern / 1e3) / 1e9,
                  "gupdates_per_s_full_square": B * N * N * Pp / (t_bp / 1e3) / 1e9,
-                 "ms_per_launch": t_bp, "slices_per_launch": B}
+                 "ms_per_launch": t_bp, "slices_per_launch": B, "variant": rg.Backprojection.variant_name(variant)}
     out["stages"] = {
         "attenuation_defects": {"ms": t_att, "gbs": att_bytes / (t_att / 1e3) / 1e9,
                                 "frac_hbm": att_bytes / (t_att / 1e3) / 1e9 / hbm},

@@ -285,12 +285,21 @@ risa_gb_status risa_gb_backprojection_autotune(risa_gb_backprojection* h, const 
                                                int* variant_out);
 risa_gb_status risa_gb_backprojection_set_variant(risa_gb_backprojection* h, int variant);
 int risa_gb_backprojection_variant_count(void);
+/* Static name of a variant ("invalid" when out of range). */
+const char* risa_gb_backprojection_variant_name(int variant);
 /* Allocates the device buffer the asynchronous variants stage from (a padded
  * (midpoint, difference) copy of the sinogram) for batches up to max_batch.
  * Set-up call: may allocate and synchronise. Autotune and the FBP engine
  * reserve for their batch themselves; an enqueue whose batch exceeds the
  * reservation runs a variant that stages windows from the sinogram itself. */
 risa_gb_status risa_gb_backprojection_reserve(risa_gb_backprojection* h, int max_batch);
+/* Measurement: runs `reps` enqueues (after one warm-up) with CUDA events on
+ * `stream` around the staging pass and around the backprojection kernel, and
+ * returns their mean durations in ms (staging 0 for unstaged variants).
+ * Synchronises. */
+risa_gb_status risa_gb_backprojection_time(risa_gb_backprojection* h, const float* sino, float* img,
+                                           int batch, int reps, void* stream, float* staging_ms,
+                                           float* kernel_ms);
 /* Synchronises and returns RISA_GB_ETIMEDOUT if a bounded device-side wait of
  * an earlier enqueue ran out (that tile's pixels were then not written). The
  * asynchronous variants stage detector windows with bulk copies completed on

@@ -129,7 +129,9 @@ int rr_filter(CUdeviceptr sino, CUdeviceptr freq, CUdeviceptr filter, int Dp, in
 }
 
 /* Backprojection::processor set-up (Backprojection.cu:118-141): the
- * __constant__ tables and scalars of the module. */
+ * __constant__ tables and scalars of the module (device symbol names; the
+ * host-side shadows of these file-scope variables carry an internal-linkage
+ * marker that the cubin's symbols do not). */
 int rr_bp_constants(const float* sin_tab, const float* cos_tab, int Pp, float norm, float scale, float center) {
    CUdeviceptr p;
    size_t bytes;
@@ -137,19 +139,19 @@ int rr_bp_constants(const float* sin_tab, const float* cos_tab, int Pp, float no
       snprintf(g_err, sizeof(g_err), "the reference's angle tables hold at most 2048 angles");
       return -1;
    }
-   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cudaL9sinLookupE"), "sinLookup") ||
+   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cuda9sinLookupE"), "sinLookup") ||
        ck(cuMemcpyHtoD(p, sin_tab, sizeof(float) * Pp), "sinLookup copy"))
       return -1;
-   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cudaL9cosLookupE"), "cosLookup") ||
+   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cuda9cosLookupE"), "cosLookup") ||
        ck(cuMemcpyHtoD(p, cos_tab, sizeof(float) * Pp), "cosLookup copy"))
       return -1;
-   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cudaL19normalizationFactorE"), "normalizationFactor") ||
+   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cuda19normalizationFactorE"), "normalizationFactor") ||
        ck(cuMemcpyHtoD(p, &norm, sizeof(float)), "norm copy"))
       return -1;
-   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cudaL5scaleE"), "scale") ||
+   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cuda5scaleE"), "scale") ||
        ck(cuMemcpyHtoD(p, &scale, sizeof(float)), "scale copy"))
       return -1;
-   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cudaL11imageCenterE"), "imageCenter") ||
+   if (ck(cuModuleGetGlobal(&p, &bytes, m_bp, "_ZN4risa4cuda11imageCenterE"), "imageCenter") ||
        ck(cuMemcpyHtoD(p, &center, sizeof(float)), "center copy"))
       return -1;
    return 0;

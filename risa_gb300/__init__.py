@@ -109,6 +109,9 @@ SIGNATURES = {
     "risa_gb_backprojection_variant_count": (_i, []),
     "risa_gb_backprojection_check": (_i, [_vp]),
     "risa_gb_backprojection_reserve": (_i, [_vp, _i]),
+    "risa_gb_backprojection_variant_name": (ctypes.c_char_p, [_i]),
+    "risa_gb_backprojection_time": (_i, [_vp, _vp, _vp, _i, _i, _vp, ctypes.POINTER(ctypes.c_float),
+                                         ctypes.POINTER(ctypes.c_float)]),
     "risa_gb_backprojection_destroy": (_i, [_vp]),
     "risa_gb_masking_create": (_i, [_vp, _vp, _pp]),
     "risa_gb_masking_workspace_bytes": (_sz, [_vp, _i]),
@@ -448,9 +451,20 @@ class Backprojection(_Handle):
         """Device buffer for the staged variants at batches up to max_batch (set-up call)."""
         _check(lib().risa_gb_backprojection_reserve(self._h, max_batch), "backprojection_reserve")
 
+    def time(self, sino, img, batch: int, reps: int = 5, stream=None):
+        """(staging ms, backprojection kernel ms), CUDA-event means over `reps` launches."""
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(lib().risa_gb_backprojection_time(self._h, ptr(sino), ptr(img), batch, reps, stream_ptr(stream),
+                                                 ctypes.byref(a), ctypes.byref(b)), "backprojection_time")
+        return a.value, b.value
+
     @staticmethod
     def variant_count() -> int:
         return lib().risa_gb_backprojection_variant_count()
+
+    @staticmethod
+    def variant_name(v: int) -> str:
+        return lib().risa_gb_backprojection_variant_name(v).decode()
 
 
 class Masking(_Handle):

@@ -44,10 +44,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
    return ok != 0;
 }
 
-// Bounded wait; returns false (and records `code` in *err) when it gives up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+// Bounded wait; returns false when it gives up.
+__device__ __forceinline__ bool mbar_wait_quiet(uint64_t* bar, uint32_t parity) {
    for (uint32_t i = 0; i < kSpinLimit; ++i)
       if (mbar_try_wait(bar, parity)) return true;
+   return false;
+}
+
+// Bounded wait; returns false (and records `code` in the global *err) when it gives up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+   if (mbar_wait_quiet(bar, parity)) return true;
    atomicCAS(err, 0, code);
    return false;
 }

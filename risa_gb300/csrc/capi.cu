@@ -217,12 +217,14 @@ struct risa_gb_filter {
    std::vector<float> h_host;  // real response [len/2+1] of a window-designed filter
    int n_taps = 0;             // > 0 for a taps-defined filter
    DevBuf h, tw;               // complex response [len], twiddles [len]
+   DevBuf twp;                 // per-pass twiddles of the radix-16 path (len 512..4096)
    FilterCfg cfg(bool adjoint = false) const {
       FilterCfg c;
       c.rows = g.Pp; c.Dp = g.Dp; c.len = len;
       c.twiddle = tw.as<float2>();
       c.h = h.as<float2>();
       c.adjoint = adjoint ? 1 : 0;
+      c.twp = twp.as<float2>();
       return c;
    }
 };
@@ -670,6 +672,7 @@ risa_gb_status risa_gb_filter_create(const risa_gb_geometry* gi, const risa_gb_p
    RG_TRY(import_params(pi, &h->p));
    RG_TRY(design_filter(h->g, h->p, &h->len, &h->h_host));
    RG_TRY(h->tw.upload(twiddles(h->len)));
+   RG_TRY(h->twp.upload(filter_pass_twiddles(h->len)));
    std::vector<float> hc(2 * (size_t)h->len, 0.f);  // real, even response as complex
    for (int k = 0; k < h->len; ++k) hc[2 * k] = h->h_host[k <= h->len / 2 ? k : h->len - k];
    RG_TRY(h->h.upload(hc));
@@ -711,6 +714,7 @@ risa_gb_status risa_gb_filter_create_taps(const risa_gb_geometry* gi, const risa
       hc[2 * k + 1] = (float)(im / len);
    }
    RG_TRY(h->tw.upload(twiddles(len)));
+   RG_TRY(h->twp.upload(filter_pass_twiddles(len)));
    RG_TRY(h->h.upload(hc));
    *out = h.release();
    return RISA_GB_OK;
@@ -791,6 +795,37 @@ static risa_gb_status bp_run(risa_gb_backprojection* h, const float* sino, float
    return RISA_GB_OK;
 }
 
+risa_gb_status risa_gb_backprojection_time(risa_gb_backprojection* h, const float* sino, float* img, int batch,
+                                           int reps, void* stream, float* staging_ms, float* kernel_ms) {
+   if (!h || !sino || !img || batch < 1 || reps < 1) return fail(RISA_GB_EINVAL, "bad timing arguments");
+   cudaStream_t st = S(stream);
+   const bool fused = h->p.masking && !h->p.normalize;
+   cudaEvent_t ev[3];
+   for (auto& e : ev) RG_CUDA(cudaEventCreate(&e));
+   RG_TRY(bp_run(h, sino, img, batch, fused, stream));  // warm-up
+   float sum_stage = 0.f, sum_kernel = 0.f;
+   risa_gb_status rc = RISA_GB_OK;
+   for (int r = 0; r < reps && rc == RISA_GB_OK; ++r) {
+      BPCfg c = h->cfg(fused);
+      c.mid_event = ev[1];
+      cudaError_t e = cudaEventRecord(ev[0], st);
+      if (e == cudaSuccess) e = launch_backprojection(sino, img, batch, c, h->variant_for(batch, fused), st);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
+      float a = 0.f, b = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&a, ev[0], ev[1]);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&b, ev[1], ev[2]);
+      if (e != cudaSuccess) rc = fail(RISA_GB_ECUDA, std::string("backprojection timing: ") + cudaGetErrorString(e));
+      sum_stage += a;
+      sum_kernel += b;
+   }
+   for (auto& e : ev) cudaEventDestroy(e);
+   if (rc != RISA_GB_OK) return rc;
+   if (staging_ms) *staging_ms = sum_stage / reps;
+   if (kernel_ms) *kernel_ms = sum_kernel / reps;
+   return risa_gb_backprojection_check(h);
+}
+
 risa_gb_status risa_gb_backprojection_reserve(risa_gb_backprojection* h, int max_batch) {
    if (!h || max_batch < 1) return fail(RISA_GB_EINVAL, "bad reserve arguments");
    return h->reserve(max_batch);
@@ -825,6 +860,7 @@ risa_gb_status risa_gb_backprojection_check(risa_gb_backprojection* h) {
 }
 
 int risa_gb_backprojection_variant_count(void) { return bp_variant_count(); }
+const char* risa_gb_backprojection_variant_name(int variant) { return bp_variant_name(variant); }
 
 risa_gb_status risa_gb_backprojection_set_variant(risa_gb_backprojection* h, int variant) {
    if (!h || variant < 0 || variant >= bp_variant_count()) return fail(RISA_GB_EINVAL, "bad variant");

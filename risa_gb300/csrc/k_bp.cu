@@ -26,17 +26,25 @@ namespace {
 // chunk. The nearest-neighbour modes always use the plain tile kernel.
 enum VariantKind { kTile, kPairs, kAsync, kAsyncPacked };
 struct BPVariant {
-   int kind, slices, achunk;
+   int kind, slices, achunk, ppt;  // ppt: pixels per thread of the staged kernels
    const char* name;
 };
 constexpr BPVariant kVariants[] = {
-    {kPairs, 2, 32, "pairs_s2_a32"},         {kPairs, 4, 16, "pairs_s4_a16"},
-    {kPairs, 4, 32, "pairs_s4_a32"},         {kPairs, 2, 16, "pairs_s2_a16"},
-    {kPairs, 1, 32, "pairs_s1_a32"},         {kTile, 0, 32, "tile32_p4_a32"},
-    {kAsync, 2, 16, "async_s2_a16"},         {kAsync, 4, 8, "async_s4_a8"},
-    {kAsync, 4, 16, "async_s4_a16"},         {kAsyncPacked, 2, 16, "async_f32x2_s2_a16"},
-    {kAsyncPacked, 2, 32, "async_f32x2_s2_a32"}, {kAsyncPacked, 4, 8, "async_f32x2_s4_a8"},
-    {kAsyncPacked, 4, 16, "async_f32x2_s4_a16"},
+    {kPairs, 2, 32, 4, "pairs_s2_a32"},
+    {kPairs, 4, 16, 4, "pairs_s4_a16"},
+    {kPairs, 2, 16, 4, "pairs_s2_a16"},
+    {kPairs, 1, 32, 4, "pairs_s1_a32"},
+    {kTile, 0, 32, 4, "tile32_p4_a32"},
+    {kAsync, 2, 16, 4, "staged_s2_a16_p4"},
+    {kAsync, 4, 8, 4, "staged_s4_a8_p4"},
+    {kAsync, 2, 16, 8, "staged_s2_a16_p8"},
+    {kAsync, 4, 8, 8, "staged_s4_a8_p8"},
+    {kAsyncPacked, 2, 16, 4, "staged_f32x2_s2_a16_p4"},
+    {kAsyncPacked, 2, 32, 4, "staged_f32x2_s2_a32_p4"},
+    {kAsyncPacked, 4, 8, 4, "staged_f32x2_s4_a8_p4"},
+    {kAsyncPacked, 4, 16, 4, "staged_f32x2_s4_a16_p4"},
+    {kAsyncPacked, 2, 16, 8, "staged_f32x2_s2_a16_p8"},
+    {kAsyncPacked, 4, 8, 8, "staged_f32x2_s4_a8_p8"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -348,20 +356,29 @@ cudaError_t launch_pairs_fit(const float* sino, float* img, int batch, const BPC
 // rounded FP64 operations), split in two:
 //
 // bp_pairs_fill writes, once per slice group, the padded pair sinogram
-//    pairs[g][angle][u][S/2] float4, u = k + win_lo over k in [-win_lo, wp - win_lo),
-// where the float4 of slices (2h, 2h+1) of bin k is
+//    pairs[g][angle][h][u] float4, u = k + win_lo over k in [-win_lo, wp - win_lo),
+// where plane h holds slices (2h, 2h+1) of the group and the float4 of bin k is
 //    (mid_2h, mid_2h+1, diff_2h, diff_2h+1),  mid = (q[k] + q[k+1]) / 2, diff = q[k+1] - q[k],
 // with q = 0 outside the detector. The padding covers every window any tile
-// of the image can request, so a window is always one contiguous run of the
-// row and is fetched with a single bulk copy.
+// of the image can request, so a window is one contiguous run of each plane
+// and is fetched with one bulk copy per plane.
 //
 // bp_linear_async: warp 0 computes the window of each angle of a chunk and
-// issues one cp.async.bulk per angle into one of two shared-memory stages,
-// completing on that stage's mbarrier; all 8 warps backproject the other
-// stage meanwhile. One CTA barrier per chunk releases a stage for refill.
-// With PACKED the two slices of a float4 are accumulated with the paired
-// FP32 instructions add/fma.rn.f32x2 (one instruction for two updates, each
-// rounded like its scalar counterpart).
+// issues the bulk copies into one of two shared-memory stages, completing on
+// that stage's mbarrier; all warps backproject the other stage meanwhile. One
+// CTA barrier per chunk releases a stage for refill.
+//
+// Shared-memory bandwidth is the bound (8 bytes of (mid, diff) per update and
+// slice), so the loads are laid out conflict-free: a 128-bit shared load is
+// served in four 8-lane phases, and each phase here covers a 4 x 2 pixel
+// block whose bins span at most 3|a| + |b| <= 6.4 window entries at 2 bins per
+// pixel -- eight distinct 16-byte entries of one 128-byte bank row. Shared
+// addresses are 32-bit, and the bin index is folded into the address from
+// the bits of the magic-rounded coordinate. With PACKED the ray coordinate is
+// carried as a duplicated pair and the two slices of a plane are accumulated
+// with add/sub/fma.rn.f32x2 (one instruction for two operations, each rounded
+// like its scalar counterpart). PPT pixels per thread (4 with 256 threads, 8
+// with 128) amortise the per-angle parameter loads.
 //
 // Every mbarrier wait is bounded; on timeout the CTA records the error in
 // cfg.err, waits (bounded) for its own copies still in flight and returns
@@ -386,7 +403,6 @@ __global__ void __launch_bounds__(256) bp_pairs_fill(const float* __restrict__ s
    const int ang = blockIdx.y, g = blockIdx.z;
    if (u >= wp) return;
    const int k = u - win_lo;
-   float4* dst = pairs + (((size_t)g * Pp + ang) * wp + u) * (S / 2);
 #pragma unroll
    for (int h = 0; h < S / 2; ++h) {
       float q[2][2];
@@ -398,8 +414,8 @@ __global__ void __launch_bounds__(256) bp_pairs_fill(const float* __restrict__ s
          q[j][0] = (live && k >= 0 && k < Dp) ? __ldg(row + k) : 0.f;
          q[j][1] = (live && k + 1 >= 0 && k + 1 < Dp) ? __ldg(row + k + 1) : 0.f;
       }
-      dst[h] = make_float4(0.5f * (q[0][0] + q[0][1]), 0.5f * (q[1][0] + q[1][1]), q[0][1] - q[0][0],
-                           q[1][1] - q[1][0]);
+      pairs[(((size_t)g * Pp + ang) * (S / 2) + h) * wp + u] =
+          make_float4(0.5f * (q[0][0] + q[0][1]), 0.5f * (q[1][0] + q[1][1]), q[0][1] - q[0][0], q[1][1] - q[1][0]);
    }
 }
 
@@ -416,18 +432,34 @@ __device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsig
    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
    return r;
 }
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+   unsigned long long r;
+   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+   return r;
+}
 __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
                                                      unsigned long long c) {
    unsigned long long r;
    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
    return r;
 }
+__device__ __forceinline__ float4 lds128(uint32_t addr) {
+   float4 v;
+   asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+   return v;
+}
+__device__ __forceinline__ ulonglong2 lds128_pairs(uint32_t addr) {
+   ulonglong2 v;
+   asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "r"(addr));
+   return v;
+}
 
-template <int S, int ACH, bool PACKED>
-__global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict__ pairs, float* __restrict__ img,
-                                                       BPCfg cfg, int wlen, int batch) {
-   constexpr int T = 32, H = S / 2;
-   extern __shared__ float4 wsm[];  // [2][ACH][wlen][H]
+template <int S, int ACH, bool PACKED, int PPT>
+__global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __restrict__ pairs,
+                                                              float* __restrict__ img, BPCfg cfg, int wlen,
+                                                              int batch) {
+   constexpr int T = 32, H = S / 2, NT = 1024 / PPT, RS = NT / 32;  // RS: rows between a thread's pixels
+   extern __shared__ float4 wsm[];  // [2][ACH][H][wlen]
    __shared__ uint64_t full[2];
    __shared__ float s_a[2][ACH], s_b[2][ACH], s_rel[2][ACH];
    __shared__ int s_fail;
@@ -436,8 +468,9 @@ __global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict_
    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
    const int g = blockIdx.z, s0 = g * S;
    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-   const int xo = (warp & 3) * 8 + (lane & 7);
-   const int yo = (warp >> 2) * 4 + (lane >> 3);
+   // 8 x 4 pixels per warp, lanes 8i..8i+7 on a 4 x 2 block
+   const int xo = (warp & 3) * 8 + (lane & 3) + ((lane >> 1) & 4);
+   const int yo = (warp >> 2) * 4 + ((lane >> 2) & 1) + ((lane >> 3) & 2);
    const float c = 0.5f * (float)(N - 1);
    const float lim = (float)N * (float)N * 0.25f;
 
@@ -449,8 +482,8 @@ __global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict_
             if (s0 + si >= batch) break;
             float* out = img + (size_t)(s0 + si) * N * N;
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-               const int x = x0 + xo, y = y0 + yo + 8 * r;
+            for (int r = 0; r < PPT; ++r) {
+               const int x = x0 + xo, y = y0 + yo + RS * r;
                if (x < N && y < N) out[(size_t)y * N + x] = cfg.mask_value;
             }
          }
@@ -459,14 +492,14 @@ __global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict_
    }
 
    const int nchunks = (Pp + ACH - 1) / ACH;
-   const size_t row_elems = (size_t)cfg.win_len * H;  // float4 per padded angle row
-   const float4* grow = pairs + (size_t)g * Pp * row_elems;
-   const uint32_t win_bytes = (uint32_t)(wlen * H * sizeof(float4));
+   const int wp = cfg.win_len;
+   const float4* grow = pairs + (size_t)g * Pp * H * wp;
+   const uint32_t plane_bytes = (uint32_t)wlen * (uint32_t)sizeof(float4);
 
    // warp 0: parameters and bulk copies of chunk ch into stage st
    auto issue = [&](int ch, int st) {
       const int na = min(ACH, Pp - ch * ACH);
-      if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)na * win_bytes);
+      if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)(na * H) * plane_bytes);
       __syncwarp();
       if (lane < na) {
          const int ang = ch * ACH + lane;
@@ -474,15 +507,17 @@ __global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict_
          double base;
          const int w0 = tile_window_start(cfg, ang, x0, y0, a, b, &base);
          int u0 = w0 + cfg.win_lo;
-         if (u0 < 0 || u0 + wlen > cfg.win_len) {  // never with host-sized padding
+         if (u0 < 0 || u0 + wlen > wp) {  // never with host-sized padding
             atomicCAS(cfg.err, 0, 4);
-            u0 = min(max(u0, 0), cfg.win_len - wlen);
+            u0 = min(max(u0, 0), wp - wlen);
          }
          s_a[st][lane] = a;
          s_b[st][lane] = b;
          s_rel[st][lane] = (float)(base - (double)w0 - 0.5);
-         async::bulk_load(wsm + ((size_t)st * ACH + lane) * wlen * H, grow + (size_t)ang * row_elems + (size_t)u0 * H,
-                          win_bytes, &full[st]);
+#pragma unroll
+         for (int h = 0; h < H; ++h)
+            async::bulk_load(wsm + ((size_t)(st * ACH + lane) * H + h) * wlen,
+                             grow + ((size_t)ang * H + h) * wp + u0, plane_bytes, &full[st]);
       }
    };
 
@@ -499,55 +534,72 @@ __global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict_
    }
    __syncthreads();
 
-   float acc[S][4];
-   unsigned long long acc2[H][4];
+   float acc[S][PPT];
+   unsigned long long acc2[H][PPT];
 #pragma unroll
-   for (int r = 0; r < 4; ++r) {
+   for (int r = 0; r < PPT; ++r) {
 #pragma unroll
       for (int si = 0; si < S; ++si) acc[si][r] = 0.f;
 #pragma unroll
       for (int h = 0; h < H; ++h) acc2[h][r] = 0ull;
    }
+   const uint32_t wbase = async::smem_u32(wsm);
    const unsigned wmax = (unsigned)(wlen - 1);
+   const unsigned long long magic2 = f2_pack(kMagic, kMagic);
 
    for (int ch = 0; ch < nchunks; ++ch) {
       const int st = ch & 1;
       if (!async::mbar_wait(&full[st], (uint32_t)((ch >> 1) & 1), cfg.err, 5)) s_fail = 1;
       const int na = min(ACH, Pp - ch * ACH);
-      const float4* wst = wsm + (size_t)st * ACH * wlen * H;
+      const uint32_t sbase = wbase + (uint32_t)(st * ACH * H) * plane_bytes;
 #pragma unroll 2
       for (int ai = 0; ai < na; ++ai) {
          const float a = s_a[st][ai], b = s_b[st][ai];
-         float tm = s_rel[st][ai] + (float)xo * a + (float)yo * b;
-         const float step = 8.f * b;
-         const float4* wa = wst + (size_t)ai * wlen * H;
+         const float t0 = s_rel[st][ai] + (float)xo * a + (float)yo * b;
+         const float step = (float)RS * b;
+         const uint32_t abase = sbase + (uint32_t)(ai * H) * plane_bytes;
+         if (PACKED) {
+            unsigned long long tm2 = f2_pack(t0, t0);
+            const unsigned long long step2 = f2_pack(step, step);
 #pragma unroll
-         for (int r = 0; r < 4; ++r) {
-            const float v = tm + kMagic;
-            const float f = tm - (v - kMagic);
-            const unsigned k = min((unsigned)(__float_as_int(v) - kMagicBits), wmax);
-            const float4* p4 = wa + (size_t)k * H;
+            for (int r = 0; r < PPT; ++r) {
+               const unsigned long long v2 = f2_add(tm2, magic2);
+               const unsigned long long f2 = f2_sub(tm2, f2_sub(v2, magic2));  // (f, f)
+               float vlo, vhi;
+               f2_unpack(v2, vlo, vhi);
+               const unsigned k = min((unsigned)(__float_as_int(vlo) - kMagicBits), wmax);
+               const uint32_t addr = abase + k * (uint32_t)sizeof(float4);
 #pragma unroll
-            for (int h = 0; h < H; ++h) {
-               if (PACKED) {
-                  const ulonglong2 p = *reinterpret_cast<const ulonglong2*>(p4 + h);
-                  acc2[h][r] = f2_fma(f2_pack(f, f), p.y, f2_add(acc2[h][r], p.x));
-               } else {
-                  const float4 p = p4[h];
+               for (int h = 0; h < H; ++h) {
+                  const ulonglong2 p = lds128_pairs(addr + (uint32_t)h * plane_bytes);
+                  acc2[h][r] = f2_fma(f2, p.y, f2_add(acc2[h][r], p.x));
+               }
+               tm2 = f2_add(tm2, step2);
+            }
+         } else {
+            float tm = t0;
+#pragma unroll
+            for (int r = 0; r < PPT; ++r) {
+               const float v = tm + kMagic;
+               const float f = tm - (v - kMagic);
+               const unsigned k = min((unsigned)(__float_as_int(v) - kMagicBits), wmax);
+               const uint32_t addr = abase + k * (uint32_t)sizeof(float4);
+#pragma unroll
+               for (int h = 0; h < H; ++h) {
+                  const float4 p = lds128(addr + (uint32_t)h * plane_bytes);
                   acc[2 * h][r] = fmaf(f, p.z, acc[2 * h][r] + p.x);
                   acc[2 * h + 1][r] = fmaf(f, p.w, acc[2 * h + 1][r] + p.y);
                }
+               tm += step;
             }
-            tm += step;
          }
       }
       __syncthreads();
       if (s_fail) {
          // drain this CTA's copies still in flight, then leave without output
          if (threadIdx.x == 0) {
-            int dummy = 0;
-            async::mbar_wait(&full[st], (uint32_t)((ch >> 1) & 1), &dummy, 1);
-            if (ch + 1 < nchunks) async::mbar_wait(&full[st ^ 1], (uint32_t)(((ch + 1) >> 1) & 1), &dummy, 1);
+            async::mbar_wait_quiet(&full[st], (uint32_t)((ch >> 1) & 1));
+            if (ch + 1 < nchunks) async::mbar_wait_quiet(&full[st ^ 1], (uint32_t)(((ch + 1) >> 1) & 1));
          }
          return;
       }
@@ -557,15 +609,15 @@ __global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict_
 #pragma unroll
       for (int h = 0; h < H; ++h)
 #pragma unroll
-         for (int r = 0; r < 4; ++r) f2_unpack(acc2[h][r], acc[2 * h][r], acc[2 * h + 1][r]);
+         for (int r = 0; r < PPT; ++r) f2_unpack(acc2[h][r], acc[2 * h][r], acc[2 * h + 1][r]);
    }
 #pragma unroll
    for (int si = 0; si < S; ++si) {
       if (s0 + si >= batch) break;
       float* out = img + (size_t)(s0 + si) * N * N;
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-         const int x = x0 + xo, y = y0 + yo + 8 * r;
+      for (int r = 0; r < PPT; ++r) {
+         const int x = x0 + xo, y = y0 + yo + RS * r;
          if (x < N && y < N) {
             float v = acc[si][r] * cfg.norm;
             if (cfg.masking) {
@@ -580,7 +632,7 @@ __global__ void __launch_bounds__(256) bp_linear_async(const float4* __restrict_
 
 inline size_t async_smem(int S, int ach, int wlen) { return 2 * sizeof(float2) * (size_t)S * ach * wlen; }
 
-template <int S, int ACH, bool PACKED>
+template <int S, int ACH, bool PACKED, int PPT>
 cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& cfg, cudaStream_t st) {
    const int wlen = window_len(cfg.scale, 32, 32);
    const size_t smem = async_smem(S, ACH, wlen);
@@ -594,26 +646,27 @@ cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& 
        sino, reinterpret_cast<float4*>(cfg.pairs), batch, cfg.Pp, cfg.Dp, cfg.win_lo, cfg.win_len);
    cudaError_t e = cudaGetLastError();
    if (e != cudaSuccess) return e;
-   auto kern = bp_linear_async<S, ACH, PACKED>;
+   if (cfg.mid_event && (e = cudaEventRecord(cfg.mid_event, st)) != cudaSuccess) return e;
+   auto kern = bp_linear_async<S, ACH, PACKED, PPT>;
    if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
    }
    dim3 grid((cfg.N + 31) / 32, (cfg.N + 31) / 32, groups);
-   kern<<<grid, 256, smem, st>>>(reinterpret_cast<const float4*>(cfg.pairs), img, cfg, wlen, batch);
+   kern<<<grid, 1024 / PPT, smem, st>>>(reinterpret_cast<const float4*>(cfg.pairs), img, cfg, wlen, batch);
    return cudaGetLastError();
 }
 
-template <int S, bool PACKED>
+template <int S, bool PACKED, int PPT>
 cudaError_t launch_async_fit(const float* sino, float* img, int batch, const BPCfg& cfg, int ach,
                              cudaStream_t st) {
    const int wlen = window_len(cfg.scale, 32, 32);
    while (ach > 4 && async_smem(S, ach, wlen) > kMaxPairsSmem) ach /= 2;
    switch (ach) {
-      case 32: return launch_async<S, 32, PACKED>(sino, img, batch, cfg, st);
-      case 16: return launch_async<S, 16, PACKED>(sino, img, batch, cfg, st);
-      case 8: return launch_async<S, 8, PACKED>(sino, img, batch, cfg, st);
-      default: return launch_async<S, 4, PACKED>(sino, img, batch, cfg, st);
+      case 32: return launch_async<S, 32, PACKED, PPT>(sino, img, batch, cfg, st);
+      case 16: return launch_async<S, 16, PACKED, PPT>(sino, img, batch, cfg, st);
+      case 8: return launch_async<S, 8, PACKED, PPT>(sino, img, batch, cfg, st);
+      default: return launch_async<S, 4, PACKED, PPT>(sino, img, batch, cfg, st);
    }
 }
 
@@ -739,17 +792,31 @@ void bp_window_extent(const float* a, const float* b, const double* ad, const do
 cudaError_t launch_backprojection(const float* sino, float* img, int batch, const BPCfg& cfg,
                                   int variant, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
+   const bool staged = cfg.interp == RISA_GB_INTERP_LINEAR && variant >= 0 && variant < kNumVariants &&
+                       (kVariants[variant].kind == kAsync || kVariants[variant].kind == kAsyncPacked);
+   if (!staged && cfg.mid_event) {  // no staging pass: it takes no time
+      cudaError_t e = cudaEventRecord(cfg.mid_event, st);
+      if (e != cudaSuccess) return e;
+   }
    if (cfg.interp != RISA_GB_INTERP_LINEAR || variant < 0 || variant >= kNumVariants ||
        kVariants[variant].kind == kTile)
       return launch_interp<32, 32, 4, 32>(sino, img, batch, cfg, st);
    const BPVariant& v = kVariants[variant];
-   if (v.kind == kAsync) {
-      if (v.slices == 2) return launch_async_fit<2, false>(sino, img, batch, cfg, v.achunk, st);
-      return launch_async_fit<4, false>(sino, img, batch, cfg, v.achunk, st);
-   }
-   if (v.kind == kAsyncPacked) {
-      if (v.slices == 2) return launch_async_fit<2, true>(sino, img, batch, cfg, v.achunk, st);
-      return launch_async_fit<4, true>(sino, img, batch, cfg, v.achunk, st);
+   if (v.kind == kAsync || v.kind == kAsyncPacked) {
+      const bool pk = v.kind == kAsyncPacked;
+      const int ach = v.achunk;
+      if (v.ppt == 8) {
+         if (v.slices == 2)
+            return pk ? launch_async_fit<2, true, 8>(sino, img, batch, cfg, ach, st)
+                      : launch_async_fit<2, false, 8>(sino, img, batch, cfg, ach, st);
+         return pk ? launch_async_fit<4, true, 8>(sino, img, batch, cfg, ach, st)
+                   : launch_async_fit<4, false, 8>(sino, img, batch, cfg, ach, st);
+      }
+      if (v.slices == 2)
+         return pk ? launch_async_fit<2, true, 4>(sino, img, batch, cfg, ach, st)
+                   : launch_async_fit<2, false, 4>(sino, img, batch, cfg, ach, st);
+      return pk ? launch_async_fit<4, true, 4>(sino, img, batch, cfg, ach, st)
+                : launch_async_fit<4, false, 4>(sino, img, batch, cfg, ach, st);
    }
    switch (v.slices) {
       case 1: return launch_pairs_fit<1>(sino, img, batch, cfg, v.achunk, st);

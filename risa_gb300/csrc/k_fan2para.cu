@@ -15,8 +15,9 @@ namespace risa_gb {
 
 namespace {
 constexpr int kThreads = 256;
-// 48 table bytes per output and plane are read once per this many frames
-constexpr int kFramesPerThread = 32;
+// 48 table bytes per output and plane are read once per this many frames; the
+// frame loop is fully unrolled so all their gathers are in flight together
+constexpr int kFramesPerThread = 8;
 
 __device__ __forceinline__ float bilinear(const float* __restrict__ f, uint32_t pk, float u, float v,
                                           int Pf, int Df) {
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(kThreads) fan2para_gather(const float* __restr
    const int na = (int)(pk[0] >> 31) + (int)(pk[1] >> 31);
    const int nb = (int)(pk[2] >> 31) + (int)(pk[3] >> 31);
    const size_t fs = (size_t)cfg.Pf * cfg.Df;
-#pragma unroll 2
+#pragma unroll
    for (int m = 0; m < kFramesPerThread; ++m) {
       const int f = first + m * step;
       if (f >= batch) break;

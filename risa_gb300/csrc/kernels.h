@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 
 namespace risa_gb {
 
@@ -130,7 +131,12 @@ struct FilterCfg {
    const float2* twiddle;  // [len] exp(-2 pi i k / len)
    const float2* h;        // [len] frequency response (Hermitian: the filter taps are real)
    int adjoint;            // multiply by conj(h): the transposed filter
+   const float2* twp = nullptr;  // radix-16 path (len 512..4096): filter_pass_twiddles(len)
 };
+// Per-pass twiddles of the radix-16 filter path, built in FP64: pass 2 as
+// [R2][16], then pass 3 as [R3][16*R2], entry [r][k] = exp(-2 pi i k r / (NS R)).
+// Empty for lengths the path does not cover.
+std::vector<float2> filter_pass_twiddles(int len);
 cudaError_t launch_filter(float* sino, int batch, const FilterCfg& cfg, cudaStream_t st);
 // Gradient of a loss with respect to the filter taps: the circular
 // cross-correlation of g (gradient at the filter output) with x (filter input)
@@ -160,6 +166,9 @@ struct BPCfg {
    size_t pairs_bytes = 0;
    int win_lo = 0, win_len = 0;
    int* err = nullptr;  // device flag: nonzero after a bounded wait gave up
+   // host side only: recorded on the stream after the staging pass and before
+   // the backprojection kernel (timing of the two separately)
+   cudaEvent_t mid_event = nullptr;
 };
 int bp_variant_count();
 const char* bp_variant_name(int v);

@@ -29,7 +29,7 @@ from oracle import ref_kernels as rk  # noqa: E402
 MAX_REL = 1e-5
 BLOCK = 16  # blockSize2D of the reference's example configuration
 
-ROFEX_F2P = dict(n_planes=2, n_fan_det=432, n_fan_proj=500, n_par_proj=32, n_par_det=48,
+ROFEX_F2P = dict(n_planes=2, n_fan_det=432, n_fan_proj=500, n_par_proj=32, n_par_det=48, n_pixels=64,
                  source_offset=23.2, detector_diameter=216.0, image_center_x=0.0, image_center_y=0.0,
                  image_width=190.0, source_diameter=[365.0, 370.0], delta_x=[815.0, 815.0],
                  delta_z=[1417.0, 1430.0], source_angle=[240.0, 240.0])
