@@ -1,6 +1,7 @@
 // C ABI: stage handles, the batched whole-chain engine with CUDA-graph
 // capture, and the host-buffer pipeline. Each stage handle replaces one of the
 // reference's stage classes (see include/risa_gb300.h for the mapping).
+#include "capi_util.h"
 #include "kernels.h"
 #include "risa_gb_internal.h"
 #include "toeplitz.h"
@@ -29,55 +30,7 @@ risa_gb_status fail(risa_gb_status code, const std::string& msg) {
    return code;
 }
 
-#define RG_CUDA(expr)                                                                         \
-   do {                                                                                       \
-      cudaError_t e_ = (expr);                                                                \
-      if (e_ != cudaSuccess)                                                                  \
-         return ::risa_gb::fail(RISA_GB_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
-   } while (0)
-
-#define RG_TRY(expr)                        \
-   do {                                     \
-      risa_gb_status s_ = (expr);           \
-      if (s_ != RISA_GB_OK) return s_;      \
-   } while (0)
-
 namespace {
-// Device allocation owned by a handle.
-struct DevBuf {
-   void* p = nullptr;
-   size_t bytes = 0;
-   DevBuf() = default;
-   DevBuf(const DevBuf&) = delete;
-   DevBuf& operator=(const DevBuf&) = delete;
-   ~DevBuf() { release(); }
-   void release() {
-      if (p) cudaFree(p);
-      p = nullptr;
-      bytes = 0;
-   }
-   risa_gb_status alloc(size_t n) {
-      release();
-      if (n == 0) return RISA_GB_OK;
-      cudaError_t e = cudaMalloc(&p, n);
-      if (e != cudaSuccess) {
-         p = nullptr;
-         return fail(RISA_GB_ENOMEM, std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
-      }
-      bytes = n;
-      return RISA_GB_OK;
-   }
-   template <typename T>
-   risa_gb_status upload(const std::vector<T>& v) {
-      RG_TRY(alloc(sizeof(T) * v.size()));
-      if (!v.empty()) RG_CUDA(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
-      return RISA_GB_OK;
-   }
-   template <typename T>
-   T* as() const { return static_cast<T*>(p); }
-};
-
-inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
 
 risa_gb_status check_layout(const Geometry& g, const Params& p) {
    if (p.module_major && (g.modules < 1 || g.Df % g.modules != 0))
