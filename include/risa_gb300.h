@@ -356,6 +356,50 @@ risa_gb_status risa_gb_fbp_intermediates(risa_gb_fbp* h, float** fan, float** pa
 risa_gb_backprojection* risa_gb_fbp_backprojection(risa_gb_fbp* h);
 risa_gb_status risa_gb_fbp_destroy(risa_gb_fbp* h);
 
+/* ---------------------------------------------------------------------------
+ * Uneven sweep: many independent parallel-beam reconstructions of different
+ * shapes in ONE persistent launch. No counterpart in the reference (one fixed
+ * geometry per pipeline); each instance runs the reference's chain in NONE
+ * mode: repair of the known defective detector columns (run rule of
+ * interpolationFunctions.h:73-97), attenuation -log((raw - dark)/(ref - dark))
+ * with a flat field (Attenuation.cu:416-444), ramp-family filter zero padded
+ * to a power of two >= 2 n_par_det (512 .. 4096; Filter.cu:169-191), linear
+ * backprojection (Backprojection.cu:238-271) and the circular mask
+ * (Masking.cu:157-169). */
+typedef struct risa_gb_sweep_instance {
+   int n_pixels;            /* image side N */
+   int n_par_proj;          /* angles over 180 degrees */
+   int n_par_det;           /* rays */
+   int filter_type;         /* RISA_GB_FILTER_* */
+   double cutoff;           /* relative cutoff frequency, (0, 1] */
+   double rotation_offset;  /* degrees */
+   double ref_level;        /* flat-field counts (reference) */
+   double dark_level;       /* dark counts */
+   int masking;             /* circular mask */
+   double masking_value;
+   const uint8_t* defect_map; /* host [n_par_det], nonzero = defective column; NULL = none */
+} risa_gb_sweep_instance;
+typedef struct risa_gb_sweep risa_gb_sweep;
+/* Builds every instance's tables (FP64 on the host) and the work list. */
+risa_gb_status risa_gb_sweep_create(const risa_gb_sweep_instance* inst, int n, risa_gb_sweep** out);
+/* Packed layouts of the inputs (uint16 [Pp][Dp] per instance) and outputs
+ * (float [N][N]): element offsets of each instance and the totals. Any
+ * pointer may be NULL. */
+risa_gb_status risa_gb_sweep_layout(const risa_gb_sweep* h, size_t* raw_offsets, size_t* img_offsets,
+                                    size_t* raw_total, size_t* img_total);
+/* One persistent launch over every instance (device buffers, packed as above). */
+risa_gb_status risa_gb_sweep_enqueue(risa_gb_sweep* h, const uint16_t* raw, float* img, void* stream);
+/* Synchronises; per instance the %globaltimer time (ns) its first row group
+ * started and its last tile finished in the last enqueue, and the launch's
+ * earliest CTA start. Any pointer may be NULL. */
+risa_gb_status risa_gb_sweep_times(risa_gb_sweep* h, uint64_t* first_ns, uint64_t* done_ns,
+                                   uint64_t* launch_ns);
+/* Synchronises; RISA_GB_ETIMEDOUT if a bounded device-side wait ran out. */
+risa_gb_status risa_gb_sweep_check(risa_gb_sweep* h);
+/* CTAs of the last persistent launch. */
+int risa_gb_sweep_grid(const risa_gb_sweep* h);
+risa_gb_status risa_gb_sweep_destroy(risa_gb_sweep* h);
+
 #ifdef __cplusplus
 }
 #endif

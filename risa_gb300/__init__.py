@@ -47,6 +47,16 @@ class Geometry(ctypes.Structure):
     ]
 
 
+class SweepInstance(ctypes.Structure):
+    """Mirror of risa_gb_sweep_instance."""
+    _fields_ = [
+        ("n_pixels", ctypes.c_int32), ("n_par_proj", ctypes.c_int32), ("n_par_det", ctypes.c_int32),
+        ("filter_type", ctypes.c_int32), ("cutoff", ctypes.c_double), ("rotation_offset", ctypes.c_double),
+        ("ref_level", ctypes.c_double), ("dark_level", ctypes.c_double), ("masking", ctypes.c_int32),
+        ("masking_value", ctypes.c_double), ("defect_map", ctypes.c_void_p),
+    ]
+
+
 class Params(ctypes.Structure):
     """Mirror of risa_gb_params."""
     _fields_ = [
@@ -127,6 +137,13 @@ SIGNATURES = {
     "risa_gb_fbp_intermediates": (_i, [_vp, _pp, _pp]),
     "risa_gb_fbp_backprojection": (_vp, [_vp]),
     "risa_gb_fbp_destroy": (_i, [_vp]),
+    "risa_gb_sweep_create": (_i, [_vp, _i, _pp]),
+    "risa_gb_sweep_layout": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "risa_gb_sweep_enqueue": (_i, [_vp, _vp, _vp, _vp]),
+    "risa_gb_sweep_times": (_i, [_vp, _vp, _vp, _vp]),
+    "risa_gb_sweep_check": (_i, [_vp]),
+    "risa_gb_sweep_grid": (_i, [_vp]),
+    "risa_gb_sweep_destroy": (_i, [_vp]),
 }
 
 _lib = None
@@ -532,3 +549,72 @@ class FBP(_Handle):
 
     def backprojection(self) -> Backprojection:
         return Backprojection(self.geom, self.params, handle=lib().risa_gb_fbp_backprojection(self._h))
+
+
+class Sweep(_Handle):
+    """Many parallel-beam reconstructions of different shapes in one persistent launch.
+
+    instances: sequence of dicts with keys n_pixels, n_par_proj, n_par_det and
+    optionally filter_type ("ramp", ...), cutoff, rotation_offset, ref_level,
+    dark_level, masking, masking_value, defect_map (uint8 array [n_par_det]).
+    Inputs and outputs are packed device buffers (see layout()).
+    """
+    _destroy = "risa_gb_sweep_destroy"
+
+    def __init__(self, instances):
+        super().__init__()
+        import numpy as np
+
+        n = len(instances)
+        arr = (SweepInstance * n)()
+        self._maps = []
+        for i, d in enumerate(instances):
+            s = arr[i]
+            s.n_pixels, s.n_par_proj, s.n_par_det = d["n_pixels"], d["n_par_proj"], d["n_par_det"]
+            ft = d.get("filter_type", "ramp")
+            s.filter_type = FILTERS[ft] if isinstance(ft, str) else int(ft)
+            s.cutoff = d.get("cutoff", 1.0)
+            s.rotation_offset = d.get("rotation_offset", 0.0)
+            s.ref_level = d.get("ref_level", 40200.0)
+            s.dark_level = d.get("dark_level", 200.0)
+            s.masking = int(d.get("masking", True))
+            s.masking_value = d.get("masking_value", 0.0)
+            m = d.get("defect_map")
+            if m is not None:
+                m = np.ascontiguousarray(m, dtype=np.uint8)
+                self._maps.append(m)
+                s.defect_map = m.ctypes.data
+            else:
+                s.defect_map = None
+        self.n = n
+        _check(lib().risa_gb_sweep_create(arr, n, ctypes.byref(self._h)), "sweep_create")
+
+    def layout(self):
+        """(raw offsets, image offsets, raw total, image total) in elements."""
+        import numpy as np
+
+        ro = np.zeros(self.n, np.uint64)
+        io = np.zeros(self.n, np.uint64)
+        rt, it = ctypes.c_size_t(), ctypes.c_size_t()
+        _check(lib().risa_gb_sweep_layout(self._h, ro.ctypes.data, io.ctypes.data, ctypes.byref(rt),
+                                          ctypes.byref(it)), "sweep_layout")
+        return ro.astype(np.int64), io.astype(np.int64), rt.value, it.value
+
+    def enqueue(self, raw, img, stream=None):
+        _check(lib().risa_gb_sweep_enqueue(self._h, ptr(raw), ptr(img), stream_ptr(stream)), "sweep_enqueue")
+
+    def times(self):
+        """(first_ns[n], done_ns[n], launch_ns) of the last enqueue (%globaltimer)."""
+        import numpy as np
+
+        f = np.zeros(self.n, np.uint64)
+        d = np.zeros(self.n, np.uint64)
+        t = ctypes.c_uint64()
+        _check(lib().risa_gb_sweep_times(self._h, f.ctypes.data, d.ctypes.data, ctypes.byref(t)), "sweep_times")
+        return f, d, t.value
+
+    def check(self):
+        _check(lib().risa_gb_sweep_check(self._h), "sweep_check")
+
+    def grid(self) -> int:
+        return lib().risa_gb_sweep_grid(self._h)

@@ -109,54 +109,66 @@ __global__ void defect_flags(const ColStats* __restrict__ st, DefectCfg cfg,
    __syncthreads();
    if (flags_out)
       for (int d = threadIdx.x; d < D; d += blockDim.x) flags_out[(size_t)f * D + d] = flags[d];
-   if (threadIdx.x != 0) return;
-
-   // Ordered run list (single thread; a handful of runs per frame).
    DefectRun* out = runs + (size_t)f * cfg.max_runs;
-   int n = 0;
    const unsigned uD = (unsigned)D;
-   if (cfg.quirk == RISA_GB_QUIRKS_RISA) {
-      // interpolationFunctions.h:76-96: flags[D] reads as 0
-      unsigned det = 0;
-      while (det < uD) {
-         if (flags[det]) {
-            const unsigned det0 = det;
-            while (flags[det] && flags[(det + 1u) % uD]) det++;
-            if (n < cfg.max_runs) {
-               DefectRun r;
-               r.start = (uint16_t)det0;
-               r.len = (uint16_t)(det - det0 + 1u);
-               r.left = (uint16_t)((det0 - 1u) % uD);
-               r.right = (uint16_t)((det + 1u) % uD);
-               out[n] = r;
-            }
-            ++n;
-         }
-         det++;
+   if (cfg.quirk != RISA_GB_QUIRKS_RISA) {
+      // NONE mode: the runs are the maximal circular sequences of flagged
+      // columns between good columns. They do not overlap and each is repaired
+      // from its own good neighbours, so they are found in parallel (a run
+      // starts at a flagged column after a good one) and their order in the
+      // list does not change the repaired frame. At most D/2 runs exist, below
+      // max_runs.
+      __shared__ int s_runs, s_good;
+      if (threadIdx.x == 0) {
+         s_runs = 0;
+         s_good = 0;
       }
-   } else {
-      unsigned start = uD;
-      for (unsigned d = 0; d < uD; ++d)
-         if (!flags[d]) { start = d; break; }
-      if (start < uD) {
-         unsigned k = 1;
-         while (k <= uD) {
-            const unsigned d = (start + k) % uD;
-            if (!flags[d]) { ++k; continue; }
-            unsigned len = 0;
-            while (flags[(start + k + len) % uD]) ++len;
-            if (n < cfg.max_runs) {
+      __syncthreads();
+      for (int d = threadIdx.x; d < D; d += blockDim.x)
+         if (!flags[d]) s_good = 1;
+      __syncthreads();
+      if (s_good) {  // with every column defective there is nothing to repair from
+         for (unsigned d = threadIdx.x; d < uD; d += blockDim.x) {
+            if (!flags[d] || flags[d == 0 ? uD - 1u : d - 1u]) continue;
+            unsigned len = 1;
+            while (flags[(d + len) % uD]) ++len;
+            const int slot = atomicAdd(&s_runs, 1);
+            if (slot < cfg.max_runs) {
                DefectRun r;
                r.start = (uint16_t)d;
                r.len = (uint16_t)len;
-               r.left = (uint16_t)((start + k - 1u) % uD);
-               r.right = (uint16_t)((start + k + len) % uD);
-               out[n] = r;
+               r.left = (uint16_t)(d == 0 ? uD - 1u : d - 1u);
+               r.right = (uint16_t)((d + len) % uD);
+               out[slot] = r;
             }
-            ++n;
-            k += len;
          }
       }
+      __syncthreads();
+      if (threadIdx.x == 0) counts[f] = s_runs < cfg.max_runs ? s_runs : cfg.max_runs;
+      return;
+   }
+   if (threadIdx.x != 0) return;
+
+   // RISA mode: ordered run list of the reference's linear scan (single thread,
+   // its continuation rule and unsigned wraps reproduced exactly).
+   int n = 0;
+   // interpolationFunctions.h:76-96: flags[D] reads as 0
+   unsigned det = 0;
+   while (det < uD) {
+      if (flags[det]) {
+         const unsigned det0 = det;
+         while (flags[det] && flags[(det + 1u) % uD]) det++;
+         if (n < cfg.max_runs) {
+            DefectRun r;
+            r.start = (uint16_t)det0;
+            r.len = (uint16_t)(det - det0 + 1u);
+            r.left = (uint16_t)((det0 - 1u) % uD);
+            r.right = (uint16_t)((det + 1u) % uD);
+            out[n] = r;
+         }
+         ++n;
+      }
+      det++;
    }
    counts[f] = n < cfg.max_runs ? n : cfg.max_runs;
 }

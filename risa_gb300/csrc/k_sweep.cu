@@ -1,0 +1,359 @@
+// Uneven sweep in one persistent launch (see sweep.h for the work model).
+//
+// Row item (256 threads): repaired counts -> attenuation -> radix-16 FFT
+// filter of 8192/LEN rows (the shared core of the filter kernel) -> the
+// padded (midpoint, difference) rows the tile items stage from. Tile item
+// (256 threads, one 32 x 32 tile, one slice): windows of 32 angles per chunk
+// fetched by cp.async.bulk into two mbarrier-completed stages, 8-byte
+// (mid, diff) records, 4 x 2-pixel load phases, magic-constant rounding as in
+// the backprojection kernels, fused circular mask.
+#include <algorithm>
+#include <cmath>
+
+#include "async_copy.h"
+#include "fft_r16.cuh"
+#include "kernels.h"
+#include "sweep.h"
+
+namespace risa_gb {
+
+namespace {
+using namespace fft;
+
+constexpr int kNT = 256;
+constexpr float kSweepMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kSweepMagicBits = 0x4B400000;
+constexpr float kAttClamp = 1e-5f;          // the reference's `temp` (Attenuation.cu:144)
+constexpr uint32_t kDepPolls = 1u << 21;    // x ~256 ns: about half a second
+
+__device__ __forceinline__ unsigned long long global_ns() {
+   unsigned long long t;
+   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+   return t;
+}
+
+__device__ __forceinline__ int load_acquire(const int* p) {
+   int v;
+   asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+   return v;
+}
+
+__device__ __forceinline__ float2 lds64(uint32_t addr) {
+   float2 v;
+   asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+   return v;
+}
+
+// Attenuation of column n of a raw row after the defect repair of that column.
+__device__ __forceinline__ float sweep_sample(const uint16_t* __restrict__ row, const SweepRepair* __restrict__ rep,
+                                              int n, float dark, float logden) {
+   unsigned raw = row[n];
+   if (rep) {
+      const SweepRepair r = rep[n];
+      if (r.len) raw = defect_value(row[r.left], row[r.right], r.m, r.len, 0);
+   }
+   float num = __fsub_rn((float)raw, dark);
+   if (num < kAttClamp) num = kAttClamp;
+   return __fsub_rn(logden, logf(num));
+}
+
+template <int LEN>
+__device__ __forceinline__ const float2* pass_twiddles(const SweepArgs& A) {
+   return A.twp[LEN == 512 ? 0 : LEN == 1024 ? 1 : LEN == 2048 ? 2 : 3];
+}
+
+// One row item: rows 2 (index FPB + local) and +1 of the instance, FPB = 4096 / LEN.
+template <int LEN>
+__device__ void sweep_rows(const SweepArgs& A, const SweepInst& I, int index, float2* sm) {
+   constexpr int TPF = LEN / 16, FPB = kNT / TPF, PL = LEN + LEN / 16;
+   using P = R16Plan<LEN>;
+   const int local = threadIdx.x / TPF, lt = threadIdx.x % TPF;
+   const int pair = index * FPB + local;
+   const int ra = 2 * pair, rb = ra + 1;
+   const bool has_a = ra < I.Pp, has_b = rb < I.Pp;
+   const int Dp = I.Dp;
+   const uint16_t* raw = A.raw + I.raw_off;
+   const uint16_t* row_a = raw + (size_t)(has_a ? ra : 0) * Dp;
+   const uint16_t* row_b = raw + (size_t)(has_b ? rb : 0) * Dp;
+   float2* buf = sm + local * PL;
+   float2 v[16];
+#pragma unroll
+   for (int r = 0; r < 16; ++r) {
+      const int n = lt + r * TPF;
+      const bool in = n < Dp;
+      v[r] = make_float2((has_a && in) ? sweep_sample(row_a, I.repair, n, I.dark, I.logden) : 0.f,
+                         (has_b && in) ? sweep_sample(row_b, I.repair, n, I.dark, I.logden) : 0.f);
+   }
+   r16_filter_core<LEN>(v, buf, lt, pass_twiddles<LEN>(A), I.h, false);
+   __syncthreads();  // the core's last pass still read buf
+   float* qa = reinterpret_cast<float*>(buf);  // filtered row a [Dp], then row b [Dp]
+   float* qb = qa + Dp;
+#pragma unroll
+   for (int b = 0; b < 16 / P::R3; ++b)
+#pragma unroll
+      for (int r = 0; r < P::R3; ++r) {
+         const int n = r16_time_index<LEN>(lt, b, r);
+         if (n < Dp) {
+            qa[n] = v[b * P::R3 + r].x;
+            qb[n] = -v[b * P::R3 + r].y;
+         }
+      }
+   __syncthreads();
+   float2* pa = A.pairs + I.pair_off + (size_t)ra * I.win_len;
+   for (int u = lt; u < I.win_len; u += TPF) {
+      const int k = u - I.win_lo;
+      const bool k0 = k >= 0 && k < Dp, k1 = k + 1 >= 0 && k + 1 < Dp;
+      if (has_a) {
+         const float q0 = k0 ? qa[k] : 0.f, q1 = k1 ? qa[k + 1] : 0.f;
+         pa[u] = make_float2(0.5f * (q0 + q1), q1 - q0);
+      }
+      if (has_b) {
+         const float q0 = k0 ? qb[k] : 0.f, q1 = k1 ? qb[k + 1] : 0.f;
+         pa[I.win_len + u] = make_float2(0.5f * (q0 + q1), q1 - q0);
+      }
+   }
+}
+
+struct TileShared {
+   float a[2][kSweepACH], b[2][kSweepACH], rel[2][kSweepACH];
+   int ok, fail;
+};
+
+// One 32 x 32 tile of instance `inst`. Returns false (uniformly) when a
+// bounded wait gave up; the CTA then stops taking items.
+__device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& I, int inst, int tile, float2* wsm,
+                           uint64_t* full, uint32_t (&uses)[2], TileShared& S) {
+   constexpr int T = 32, PPT = 4, RS = 8;
+   const int N = I.N, Pp = I.Pp, W = I.wlen2;
+   const int x0 = (tile % I.tiles_x) * T, y0 = (tile / I.tiles_x) * T;
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int xo = (warp & 3) * 8 + (lane & 3) + ((lane >> 1) & 4);
+   const int yo = (warp >> 2) * 4 + ((lane >> 2) & 1) + ((lane >> 3) & 2);
+   const float c = 0.5f * (float)(N - 1);
+   const float lim = (float)N * (float)N * 0.25f;
+   float* out = A.img + I.img_off;
+
+   bool skip = false;
+   if (I.masking) {
+      const float nx = fminf(fmaxf(c, (float)x0), (float)(x0 + T - 1)) - c;
+      const float ny = fminf(fmaxf(c, (float)y0), (float)(y0 + T - 1)) - c;
+      skip = nx * nx + ny * ny > lim;
+   }
+   if (skip) {
+#pragma unroll
+      for (int r = 0; r < PPT; ++r) {
+         const int x = x0 + xo, y = y0 + yo + RS * r;
+         if (x < N && y < N) out[(size_t)y * N + x] = I.mask_value;
+      }
+   } else {
+      // every row item of the instance must have been written
+      if (threadIdx.x == 0) {
+         int ok = 0;
+         for (uint32_t i = 0; i < kDepPolls; ++i) {
+            if (load_acquire(A.rows_done + inst) >= I.row_items) {
+               ok = 1;
+               break;
+            }
+            __nanosleep(256);
+         }
+         if (!ok) atomicCAS(A.err, 0, 7);
+         S.ok = ok;
+         S.fail = 0;
+      }
+      __syncthreads();
+      if (!S.ok) return false;
+      // the rows were written by generic-proxy stores of other CTAs; the bulk
+      // copies below read them through the async proxy
+      if (warp == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
+      const float2* prow = A.pairs + I.pair_off;
+      const uint32_t win_bytes = (uint32_t)W * (uint32_t)sizeof(float2);
+      const int nchunks = (Pp + kSweepACH - 1) / kSweepACH;
+      auto issue = [&](int ch, int st) {
+         const int na = min(kSweepACH, Pp - ch * kSweepACH);
+         if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)na * win_bytes);
+         __syncwarp();
+         if (lane < na) {
+            const int ang = ch * kSweepACH + lane;
+            const float a = __ldg(I.a + ang), b = __ldg(I.b + ang);
+            const double base = __dadd_rn(__dadd_rn(__ldg(I.t0 + ang), __dmul_rn((double)x0, __ldg(I.ad + ang))),
+                                          __dmul_rn((double)y0, __ldg(I.bd + ang)));
+            const double tmin = __dadd_rn(__dadd_rn(base, (double)fminf(0.f, __fmul_rn(31.f, a))),
+                                          (double)fminf(0.f, __fmul_rn(31.f, b)));
+            const int w0 = ((int)floor(tmin) - 2) & ~1;  // even start: 16-byte aligned copies
+            int u0 = w0 + I.win_lo;
+            if (u0 < 0 || u0 + W > I.win_len) {  // never with host-sized padding
+               atomicCAS(A.err, 0, 4);
+               u0 = min(max(u0, 0), I.win_len - W) & ~1;
+            }
+            S.a[st][lane] = a;
+            S.b[st][lane] = b;
+            S.rel[st][lane] = (float)(base - (double)w0 - 0.5);
+            async::bulk_load(wsm + (size_t)(st * kSweepACH + lane) * W, prow + (size_t)ang * I.win_len + u0,
+                             win_bytes, &full[st]);
+         }
+      };
+      if (warp == 0) {
+         issue(0, 0);
+         if (nchunks > 1) issue(1, 1);
+      }
+      __syncthreads();
+
+      float acc[PPT];
+#pragma unroll
+      for (int r = 0; r < PPT; ++r) acc[r] = 0.f;
+      const uint32_t wbase = async::smem_u32(wsm);
+      const unsigned wmax = (unsigned)(W - 1);
+      bool failed = false;
+      for (int ch = 0; ch < nchunks; ++ch) {
+         const int st = ch & 1;
+         if (!async::mbar_wait(&full[st], uses[st] & 1u, A.err, 5)) S.fail = 1;
+         ++uses[st];
+         const int na = min(kSweepACH, Pp - ch * kSweepACH);
+#pragma unroll 2
+         for (int ai = 0; ai < na; ++ai) {
+            const float a = S.a[st][ai], b = S.b[st][ai];
+            float tm = S.rel[st][ai] + (float)xo * a + (float)yo * b;
+            const float step = (float)RS * b;
+            const uint32_t abase = wbase + (uint32_t)((st * kSweepACH + ai) * W) * (uint32_t)sizeof(float2);
+#pragma unroll
+            for (int r = 0; r < PPT; ++r) {
+               const float v = tm + kSweepMagic;
+               const float f = tm - (v - kSweepMagic);
+               const unsigned k = min((unsigned)(__float_as_int(v) - kSweepMagicBits), wmax);
+               const float2 p = lds64(abase + k * (uint32_t)sizeof(float2));
+               acc[r] = fmaf(f, p.y, acc[r] + p.x);
+               tm += step;
+            }
+         }
+         __syncthreads();
+         if (S.fail) {
+            if (threadIdx.x == 0) {  // the copies of the next chunk may still be in flight
+               if (ch + 1 < nchunks) async::mbar_wait_quiet(&full[st ^ 1], uses[st ^ 1] & 1u);
+            }
+            failed = true;
+            break;
+         }
+         if (warp == 0 && ch + 2 < nchunks) issue(ch + 2, st);
+      }
+      if (failed) return false;
+#pragma unroll
+      for (int r = 0; r < PPT; ++r) {
+         const int x = x0 + xo, y = y0 + yo + RS * r;
+         if (x < N && y < N) {
+            float val = acc[r] * I.norm;
+            if (I.masking) {
+               const float dx = (float)x - c, dy = (float)y - c;
+               if (dx * dx + dy * dy > lim) val = I.mask_value;
+            }
+            out[(size_t)y * N + x] = val;
+         }
+      }
+   }
+   __threadfence();
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      const int done = atomicAdd(A.tiles_done + inst, 1) + 1;
+      if (done == I.tiles) A.t_done[inst] = global_ns();
+   }
+   return true;
+}
+
+__global__ void __launch_bounds__(kNT, 2) sweep_persistent(SweepArgs A) {
+   extern __shared__ float4 sm4[];
+   float2* sm = reinterpret_cast<float2*>(sm4);
+   __shared__ uint64_t full[2];
+   __shared__ TileShared ts;
+   __shared__ int s_item;
+   if (threadIdx.x == 0) {
+      async::mbar_init(&full[0], 1);
+      async::mbar_init(&full[1], 1);
+      async::mbar_init_fence();
+      atomicMin(A.t_launch, global_ns());
+   }
+   __syncthreads();
+   uint32_t uses[2] = {0u, 0u};  // completed phases of each stage barrier
+   for (;;) {
+      if (threadIdx.x == 0) s_item = atomicAdd(A.next, 1);
+      __syncthreads();
+      const int item = s_item;
+      __syncthreads();
+      if (item >= A.n_items) break;
+      const SweepItem it = A.items[item];
+      const SweepInst& I = A.inst[it.inst];
+      if (it.kind == kSweepRows) {
+         if (threadIdx.x == 0) atomicMin(A.t_first + it.inst, global_ns());
+         switch (I.len) {
+            case 512: sweep_rows<512>(A, I, it.index, sm); break;
+            case 1024: sweep_rows<1024>(A, I, it.index, sm); break;
+            case 2048: sweep_rows<2048>(A, I, it.index, sm); break;
+            default: sweep_rows<4096>(A, I, it.index, sm); break;
+         }
+         __threadfence();
+         __syncthreads();
+         if (threadIdx.x == 0) atomicAdd(A.rows_done + it.inst, 1);
+      } else if (!sweep_tile(A, I, it.inst, it.index, sm, full, uses, ts)) {
+         break;
+      }
+   }
+}
+}  // namespace
+
+int sweep_window_len(float scale) {
+   // bins a 32-pixel tile spans at this scale, two bins of margin either side,
+   // plus one bin for the even-aligned start
+   return (((int)ceilf(scale * 1.41421357f * 32.f) + 6 + 3) & ~3) + 2;
+}
+
+void sweep_window_extent(const float* a, const float* b, const double* ad, const double* bd, const double* t0,
+                         int Pp, int N, int wlen2, bool masking, int* win_lo, int* win_len) {
+   // mirrors sweep_tile: window start ((floor(tmin) - 2) & ~1), tile skip test
+   // (host code is compiled without floating-point contraction)
+   const int tiles = (N + 31) / 32;
+   const double c = 0.5 * (double)(N - 1), lim = (double)N * (double)N * 0.25;
+   long lo = 0x7fffffff, hi = -0x7fffffff;
+   for (int by = 0; by < tiles; ++by)
+      for (int bx = 0; bx < tiles; ++bx) {
+         const int x0 = bx * 32, y0 = by * 32;
+         if (masking) {
+            const double nx = std::fmin(std::fmax(c, (double)x0), (double)(x0 + 31)) - c;
+            const double ny = std::fmin(std::fmax(c, (double)y0), (double)(y0 + 31)) - c;
+            if (nx * nx + ny * ny > lim * (1.0 + 1e-6) + 1.0) continue;
+         }
+         for (int i = 0; i < Pp; ++i) {
+            const double base = (t0[i] + (double)x0 * ad[i]) + (double)y0 * bd[i];
+            const float ma = 31.f * a[i], mb = 31.f * b[i];
+            const double tmin = (base + (double)std::fmin(0.f, ma)) + (double)std::fmin(0.f, mb);
+            const long w0 = ((long)std::floor(tmin) - 2) & ~1L;
+            lo = std::min(lo, w0);
+            hi = std::max(hi, w0 + wlen2);
+         }
+      }
+   if (lo > hi) lo = hi = 0;
+   // two bins of slack either side, both values even
+   *win_lo = (int)(2 - lo);
+   *win_len = (int)(hi - lo + 4);
+}
+
+size_t sweep_smem_bytes(int max_wlen2) {
+   const size_t rows = sizeof(float2) * (size_t)4352;  // 4096/LEN row pairs x (LEN + LEN/16), any LEN
+   const size_t tiles = sizeof(float2) * 2 * (size_t)kSweepACH * max_wlen2;
+   return std::max(rows, tiles);
+}
+
+cudaError_t launch_sweep(const SweepArgs& a, int max_wlen2, cudaStream_t st, int* grid_out) {
+   const size_t smem = sweep_smem_bytes(max_wlen2);
+   if (smem > 200 * 1024) return cudaErrorInvalidConfiguration;
+   cudaError_t e = cudaFuncSetAttribute(sweep_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+   if (e != cudaSuccess) return e;
+   int dev = 0, sms = 0, per_sm = 0;
+   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_persistent, kNT, smem)) != cudaSuccess)
+      return e;
+   const int grid = std::max(1, sms * std::max(1, per_sm));
+   if (grid_out) *grid_out = grid;
+   sweep_persistent<<<grid, kNT, smem, st>>>(a);
+   return cudaGetLastError();
+}
+
+}  // namespace risa_gb

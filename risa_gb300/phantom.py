@@ -202,3 +202,49 @@ def parallel_sinograms(n_slices: int, n_par_proj: int, n_par_det: int, width: fl
         phs.append(ph)
         out[i] = line_integrals_parallel(ph, th, s)
     return out, phs
+
+
+def sweep_instances(n: int, seed: int = 5, n_min: int = 128, n_max: int = 1024, pp_min: int = 180,
+                    pp_max: int = 1440, defect_max: float = 0.02, ref_level: float = 40200.0,
+                    dark_level: float = 200.0):
+    """Seeded instance list of the uneven sweep: image side log-uniform in
+    [n_min, n_max], angles uniform in [pp_min, pp_max], rays = 1.25 x the side
+    rounded to a multiple of 32, 0..defect_max defective detector columns, a
+    ramp or Hann filter, circular mask. Dicts as risa_gb300.Sweep takes them."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        side = int(round(float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))))
+        pp = int(rng.integers(pp_min, pp_max + 1))
+        dp = max(32, 32 * int(round(1.25 * side / 32.0)))
+        k = int(round(rng.uniform(0.0, defect_max) * dp))
+        dmap = np.zeros(dp, np.uint8)
+        if k:
+            cols = rng.choice(dp, size=k, replace=False)
+            dmap[cols] = 1
+        out.append(dict(n_pixels=side, n_par_proj=pp, n_par_det=dp,
+                        filter_type="ramp" if rng.uniform() < 0.5 else "hanning", cutoff=1.0,
+                        rotation_offset=0.0, ref_level=ref_level, dark_level=dark_level, masking=True,
+                        masking_value=0.0, defect_map=dmap))
+    return out
+
+
+def sweep_counts(inst: dict, seed: int, width: float = 200.0, i0: float = 40000.0) -> np.ndarray:
+    """uint16 parallel-beam counts [Pp][Dp] of one sweep instance: seeded 8-ellipse
+    phantom, Poisson(I0 exp(-integral)) + dark, defective columns dead (= dark)
+    or flickering (+-50%)."""
+    pp, dp = inst["n_par_proj"], inst["n_par_det"]
+    rng = np.random.default_rng(seed)
+    ph = random_phantom(seed, n=8, fov=width)
+    th = np.arange(pp) * np.pi / pp
+    s = (np.arange(dp) + 0.5 - dp / 2.0) * width / dp
+    raw = counts(line_integrals_parallel(ph, th, s), rng, i0, inst.get("dark_level", 200.0))
+    dmap = inst.get("defect_map")
+    if dmap is not None:
+        for col in np.flatnonzero(dmap):
+            if rng.uniform() < 0.5:
+                raw[:, col] = int(inst.get("dark_level", 200.0))
+            else:
+                f = rng.uniform(0.5, 1.5, size=pp)
+                raw[:, col] = np.clip(raw[:, col] * f, 0, 65535).astype(np.uint16)
+    return raw
