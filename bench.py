@@ -305,16 +305,11 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     filt = rg.Filter(g, p)
     bp = fbp.backprojection()
     reps = 5
-    t_att = timed(torch, stream, lambda: att.enqueue(raw[:B], fan_buf, rg.PLANES_INTERLEAVED, B, stream), reps)
-    t_f2p = timed(torch, stream, lambda: f2p.enqueue(fan_buf, par_buf, rg.PLANES_INTERLEAVED, B, stream), reps)
-    par_copy = torch.randn((B, Pp, Dp), dtype=torch.float32, device=dev)
-    t_filt = timed(torch, stream, lambda: filt.enqueue(par_copy, B, stream), reps)
-    t_bp = timed(torch, stream, lambda: bp.enqueue(par_buf, img[:B], B, stream), reps)
-    t_stage, t_kern = bp.time(par_buf, img[:B], B, reps, stream)
-    dfx_b = rg.Defects(g, p, max_batch=B)
-    ws_b = torch.empty(dfx_b.workspace_bytes(B), dtype=torch.uint8, device=dev)
-    raw_b = raw[:B].clone()
-    t_def = timed(torch, stream, lambda: dfx_b.enqueue(raw_b, B, ws_b, stream=stream), reps)
+    # the engine's own kernels on one chunk, CUDA events between them on the launch stream
+    es = fbp.time_stages(raw[:B], img[:B], rg.PLANES_INTERLEAVED, B, reps, stream)
+    t_def, t_att, t_f2p, t_filt = es["defect_detect"], es["attenuation_repair"], es["rebinning"], es["filter"]
+    t_stage, t_kern = es["bp_staging"], es["bp_kernel"]
+    t_bp = t_stage + t_kern
     fs, ps = Pf * Df, Pp * Dp
     att_bytes = B * fs * (2 + 4) + L * fs * 4
     f2p_bytes = B * (fs * 4 + ps * 4) + L * ps * 4 * 12
@@ -352,7 +347,7 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
         "filter": {"ms": t_filt, "gbs": filt_bytes / (t_filt / 1e3) / 1e9,
                    "frac_hbm": filt_bytes / (t_filt / 1e3) / 1e9 / hbm},
         "backprojection": {"ms": t_bp},
-        "defects_detect_repair": {"ms": t_def, "gbs": B * fs * 2 * 3 / (t_def / 1e3) / 1e9},
+        "defect_detect": {"ms": t_def, "gbs": B * fs * 2 / (t_def / 1e3) / 1e9},
         "hbm_peak_gbs": hbm, "batch": B,
     }
 
@@ -457,14 +452,18 @@ def measure_precision(torch, rg, dev):
     x = np.ascontiguousarray(np.concatenate([base] * (S // 8)))  # 8 distinct phantoms cycled
     g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=N)
     p = rg.make_params(filter_type="ramp", pad=pad)
-    tz, ff = rg.Toeplitz(g, p), rg.Filter(g, p)
+    tz, tz16, ff = rg.Toeplitz(g, p), rg.Toeplitz(g, p), rg.Filter(g, p)
+    tz16.set_precision(rg.SPLIT_F16X3)
     xs = torch.from_numpy(x).to(dev)
-    t_fft, t_tz = xs.clone(), xs.clone()
+    t_fft, t_tz, t_tz16 = xs.clone(), xs.clone(), xs.clone()
     ws = torch.empty(tz.workspace_bytes(S), dtype=torch.uint8, device=dev)
+    scratch = torch.empty_like(xs)
+    ms_copy = cuda_ms(torch, lambda: scratch.copy_(xs))  # the refill each timed filter call includes
     ms_fft = cuda_ms(torch, lambda: (t_fft.copy_(xs), ff.enqueue(t_fft, S)))
-    ms_copy = cuda_ms(torch, lambda: t_fft.copy_(xs))
     ms_tz = cuda_ms(torch, lambda: (t_tz.copy_(xs), tz.enqueue(t_tz, S, ws)))
+    ms_tz16 = cuda_ms(torch, lambda: (t_tz16.copy_(xs), tz16.enqueue(t_tz16, S, ws)))
     tz.check()
+    tz16.check()
     n_len, _ = ff.response()
     ho = oracle.design_filter(n_len, rg.FILTERS["ramp"], 1.0, oracle.QUIRK_NONE)
     exp_f = np.stack([oracle.filter_rows(x[b], n_len, ho) for b in range(4)])
@@ -474,7 +473,8 @@ def measure_precision(torch, rg, dev):
     og = ns_geom(Pp, Dp, N)
     exp_img = oracle.fbp_parallel(og, oracle.make_params(filter_type="ramp", pad=pad), x[:2])
     useful = 2.0 * S * Pp * Dp * Dp
-    for name, t, ms in (("fft", t_fft, ms_fft - ms_copy), ("toeplitz_split_bf16x3", t_tz, ms_tz - ms_copy)):
+    for name, t, ms in (("fft", t_fft, ms_fft - ms_copy), ("toeplitz_split_bf16x3", t_tz, ms_tz - ms_copy),
+                        ("toeplitz_split_f16x3", t_tz16, ms_tz16 - ms_copy)):
         bp.enqueue(t[:2], img, 2)
         rec = {"ms_per_64_slices": ms, "filter": err_pair(t[:4].cpu().numpy(), exp_f),
                "image": err_pair(img.cpu().numpy(), exp_img)}
@@ -529,6 +529,9 @@ def measure_differentiation(torch, rg, dev):
         filt.enqueue_adjoint(gs, S)              # d/d(sinogram)
 
     ms_f, ms_b = cuda_ms(torch, forward), cuda_ms(torch, backward)
+    ms_parts = {"bp_adjoint": cuda_ms(torch, lambda: bp.enqueue_adjoint(y, gsf, S)),
+                "taps_grad": cuda_ms(torch, lambda: filt.taps_grad(s, gsf, gt, S, ws)),
+                "filter_adjoint": cuda_ms(torch, lambda: (gs.copy_(gsf), filt.enqueue_adjoint(gs, S)))}
     forward()
     backward()
     torch.cuda.synchronize()
@@ -536,7 +539,7 @@ def measure_differentiation(torch, rg, dev):
     tr = s.double() * gs.double()
     dot = abs(float(tl.sum()) - float(tr.sum())) / max(float(tl.abs().sum()), float(tr.abs().sum()))
     return {"workload": f"{S} slices, {Pp} x {Dp} -> {N}^2, {T} filter taps", "ms_forward": ms_f,
-            "ms_backward": ms_b, "adjoint_dot_rel": dot,
+            "ms_backward": ms_b, "ms_backward_parts": ms_parts, "adjoint_dot_rel": dot,
             "fd_check": "FP64 central differences on 32 taps in tests/test_gpu_autograd.py"}
 
 

@@ -257,6 +257,12 @@ risa_gb_status risa_gb_toeplitz_enqueue(risa_gb_toeplitz* h, float* sino, int ba
 /* Synchronises and returns RISA_GB_ETIMEDOUT if a bounded device-side wait of
  * an earlier enqueue ran out (the kernel then skipped its output). */
 risa_gb_status risa_gb_toeplitz_check(risa_gb_toeplitz* h);
+/* Split of the operands: RISA_GB_SPLIT_BF16X3 (default) or RISA_GB_SPLIT_F16X3
+ * (fp16 hi + lo, each input row and T scaled by powers of two, about 22
+ * significant bits per operand instead of 16). */
+#define RISA_GB_SPLIT_BF16X3 0
+#define RISA_GB_SPLIT_F16X3 1
+risa_gb_status risa_gb_toeplitz_set_precision(risa_gb_toeplitz* h, int split);
 risa_gb_status risa_gb_toeplitz_destroy(risa_gb_toeplitz* h);
 /* Host-only filter design (no GPU). h: len/2 + 1 floats. */
 risa_gb_status risa_gb_filter_design_host(const risa_gb_geometry* g, const risa_gb_params* p,
@@ -351,8 +357,18 @@ risa_gb_status risa_gb_graph_destroy(risa_gb_graph* g);
  * copies the images back. Pinned host memory is fastest. Blocks until done. */
 risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, float* host_img,
                                     int n_frames, int plane);
-/* Per-stage access for inspection (intermediate device buffers). */
+/* Per-stage access for inspection (intermediate device buffers). The engine
+ * keeps attenuated fan frames as frame quads -- 4 frames of one plane side by
+ * side, [quad][n_fan_proj][n_fan_det][4] float, quads of plane k before those of
+ * plane k+1 -- and parallel sinograms per frame, [batch][n_par_proj][n_par_det].
+ * The fan buffer holds at least max_batch frames. */
 risa_gb_status risa_gb_fbp_intermediates(risa_gb_fbp* h, float** fan, float** par);
+/* Measurement: runs the engine's stages on one batch `reps` times (after a
+ * warm-up) with CUDA events on `stream` between them; ms[6] receives the mean
+ * durations of defect detection, attenuation (+ repair), rebinning, filter,
+ * backprojection staging and the backprojection kernel. Synchronises. */
+risa_gb_status risa_gb_fbp_time_stages(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane, int batch,
+                                       int reps, void* stream, float* ms);
 risa_gb_backprojection* risa_gb_fbp_backprojection(risa_gb_fbp* h);
 risa_gb_status risa_gb_fbp_destroy(risa_gb_fbp* h);
 

@@ -21,6 +21,7 @@ FILTER_RAMP, FILTER_SHEPP_LOGAN, FILTER_COSINE, FILTER_HAMMING, FILTER_HANNING =
 FILTERS = {"ramp": 0, "sheppLogan": 1, "cosine": 2, "hamming": 3, "hanning": 4}
 INTERP_LINEAR, INTERP_NEAREST, INTERP_NEAREST_TRUNC = 0, 1, 2
 PLANES_INTERLEAVED = -1
+SPLIT_BF16X3, SPLIT_F16X3 = 0, 1
 MAX_PLANES = 4
 
 STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported", -3: "CUDA error", -4: "timed out",
@@ -111,6 +112,7 @@ SIGNATURES = {
     "risa_gb_toeplitz_enqueue": (_i, [_vp, _vp, _i, _vp, _vp]),
     "risa_gb_toeplitz_check": (_i, [_vp]),
     "risa_gb_toeplitz_destroy": (_i, [_vp]),
+    "risa_gb_toeplitz_set_precision": (_i, [_vp, _i]),
     "risa_gb_backprojection_create": (_i, [_vp, _vp, _pp]),
     "risa_gb_backprojection_enqueue": (_i, [_vp, _vp, _vp, _i, _vp]),
     "risa_gb_backprojection_enqueue_adjoint": (_i, [_vp, _vp, _vp, _i, _vp]),
@@ -137,6 +139,7 @@ SIGNATURES = {
     "risa_gb_fbp_intermediates": (_i, [_vp, _pp, _pp]),
     "risa_gb_fbp_backprojection": (_vp, [_vp]),
     "risa_gb_fbp_destroy": (_i, [_vp]),
+    "risa_gb_fbp_time_stages": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp]),
     "risa_gb_sweep_create": (_i, [_vp, _i, _pp]),
     "risa_gb_sweep_layout": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "risa_gb_sweep_enqueue": (_i, [_vp, _vp, _vp, _vp]),
@@ -419,6 +422,10 @@ class Toeplitz(_Handle):
     def check(self):
         _check(lib().risa_gb_toeplitz_check(self._h), "toeplitz_check")
 
+    def set_precision(self, split: int):
+        """SPLIT_BF16X3 (default) or SPLIT_F16X3."""
+        _check(lib().risa_gb_toeplitz_set_precision(self._h, split), "toeplitz_set_precision")
+
 
 def filter_design_host(geom: Geometry, params: Params):
     import numpy as np
@@ -546,6 +553,16 @@ class FBP(_Handle):
         _check(lib().risa_gb_fbp_intermediates(self._h, ctypes.byref(fan), ctypes.byref(par)),
                "fbp_intermediates")
         return fan.value, par.value
+
+    def time_stages(self, raw, img, plane: int, batch: int, reps: int = 5, stream=None) -> dict:
+        """Mean ms of the engine's stages on one batch (CUDA events on the stream)."""
+        import numpy as np
+
+        ms = np.zeros(6, np.float32)
+        _check(lib().risa_gb_fbp_time_stages(self._h, ptr(raw), ptr(img), plane, batch, reps, stream_ptr(stream),
+                                             ms.ctypes.data), "fbp_time_stages")
+        keys = ("defect_detect", "attenuation_repair", "rebinning", "filter", "bp_staging", "bp_kernel")
+        return {k: float(v) for k, v in zip(keys, ms)}
 
     def backprojection(self) -> Backprojection:
         return Backprojection(self.geom, self.params, handle=lib().risa_gb_fbp_backprojection(self._h))

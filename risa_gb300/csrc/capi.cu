@@ -7,6 +7,7 @@
 #include "toeplitz.h"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -205,6 +206,7 @@ struct risa_gb_backprojection {
    // the device error flag of their bounded waits
    int win_lo[2] = {0, 0}, win_len[2] = {0, 0};
    DevBuf pairs, err;
+   DevBuf rowbase, colbase;  // adjoint: (hi, lo) line starts [Pp][N]
    BPCfg cfg(bool fused_mask) const {
       BPCfg c;
       c.Pp = g.Pp; c.Dp = g.Dp; c.N = g.N;
@@ -223,6 +225,8 @@ struct risa_gb_backprojection {
       c.win_lo = win_lo[fused_mask ? 1 : 0];
       c.win_len = win_len[fused_mask ? 1 : 0];
       c.err = err.as<int>();
+      c.rowbase = rowbase.as<float2>();
+      c.colbase = colbase.as<float2>();
       return c;
    }
    // Pair buffer for `batch` slices under every variant. Only set-up calls
@@ -737,6 +741,10 @@ risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* gi, const r
                        m == 1, &h->win_lo[m], &h->win_len[m]);
    RG_TRY(h->err.alloc(sizeof(int)));
    RG_CUDA(cudaMemset(h->err.p, 0, sizeof(int)));
+   if (h->p.interp == RISA_GB_INTERP_LINEAR) {
+      RG_TRY(h->rowbase.upload(bp_line_starts(t.t0.data(), t.bd.data(), h->g.Pp, h->g.N)));
+      RG_TRY(h->colbase.upload(bp_line_starts(t.t0.data(), t.ad.data(), h->g.Pp, h->g.N)));
+   }
    *out = h.release();
    return RISA_GB_OK;
 }
@@ -930,7 +938,11 @@ risa_gb_status risa_gb_fbp_create(const risa_gb_geometry* gi, const risa_gb_para
    RG_TRY(risa_gb_filter_create(gi, pi, &h->filt));
    RG_TRY(risa_gb_backprojection_create(gi, pi, &h->bp));
    RG_TRY(risa_gb_masking_create(gi, pi, &h->mask));
-   RG_TRY(h->fan.alloc(sizeof(float) * (size_t)max_batch * g.Pf * g.Df));
+   // attenuated frames are kept as frame quads (see QuadMap): room for the
+   // padded quads of a batch with interleaved or with fixed planes
+   const int quads = std::max(quad_count(make_quad_map(g.L, RISA_GB_PLANES_INTERLEAVED, max_batch)),
+                              quad_count(make_quad_map(g.L, 0, max_batch)));
+   RG_TRY(h->fan.alloc(sizeof(float) * 4 * (size_t)quads * g.Pf * g.Df));
    RG_TRY(h->par.alloc(sizeof(float) * (size_t)max_batch * g.Pp * g.Dp));
    if (h->defects) RG_TRY(h->dws.alloc(risa_gb_defects_workspace_bytes(h->defects, max_batch)));
    RG_TRY(h->mm.alloc(sizeof(unsigned int) * 2 * (size_t)max_batch));
@@ -951,11 +963,11 @@ risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* i
       const DefectCfg& dc = h->defects->cfg;
       DefectWorkspace ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs);
       RG_CUDA(launch_defect_detect(raw, batch, dc, ws, nullptr, st));
-      RG_CUDA(launch_attenuation(raw, fan, batch, h->atten->cfg(plane), &ws, dc.max_runs, st));
+      RG_CUDA(launch_attenuation_quads(raw, fan, batch, h->atten->cfg(plane), &ws, dc.max_runs, st));
    } else {
-      RG_CUDA(launch_attenuation(raw, fan, batch, h->atten->cfg(plane), nullptr, 0, st));
+      RG_CUDA(launch_attenuation_quads(raw, fan, batch, h->atten->cfg(plane), nullptr, 0, st));
    }
-   RG_CUDA(launch_fan2para(fan, par, batch, h->f2p->cfg(plane), st));
+   RG_CUDA(launch_fan2para_quads(fan, par, batch, h->f2p->cfg(plane), st));
    RG_CUDA(launch_filter(par, batch, h->filt->cfg(), st));
    const bool fused = h->p.masking && !h->p.normalize;
    RG_TRY(bp_run(h->bp, par, img, batch, fused, stream));
@@ -963,6 +975,57 @@ risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* i
       RG_CUDA(launch_mask(img, batch, h->g.N, (float)h->p.masking_value, 1, h->mm.as<float>(),
                           h->p.masking, st));
    return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fbp_time_stages(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane, int batch,
+                                       int reps, void* stream, float* ms) {
+   if (!h || !raw || !img || !ms || reps < 1) return fail(RISA_GB_EINVAL, "bad timing arguments");
+   if (batch < 1 || batch > h->max_batch) return fail(RISA_GB_EINVAL, "batch exceeds max_batch");
+   RG_TRY(check_plane(h->g, plane));
+   RG_TRY(risa_gb_fbp_enqueue(h, raw, img, plane, batch, stream));  // warm-up
+   cudaStream_t st = S(stream);
+   float* fan = h->fan.as<float>();
+   float* par = h->par.as<float>();
+   const bool fused = h->p.masking && !h->p.normalize;
+   cudaEvent_t ev[7];
+   for (auto& e : ev) RG_CUDA(cudaEventCreate(&e));
+   double sum[6] = {0, 0, 0, 0, 0, 0};
+   risa_gb_status rc = RISA_GB_OK;
+   for (int r = 0; r < reps && rc == RISA_GB_OK; ++r) {
+      cudaError_t e = cudaEventRecord(ev[0], st);
+      DefectWorkspace ws{};
+      if (e == cudaSuccess && h->defects) {
+         const DefectCfg& dc = h->defects->cfg;
+         ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs);
+         e = launch_defect_detect(raw, batch, dc, ws, nullptr, st);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+      if (e == cudaSuccess)
+         e = launch_attenuation_quads(raw, fan, batch, h->atten->cfg(plane), h->defects ? &ws : nullptr,
+                                      h->defects ? h->defects->cfg.max_runs : 0, st);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
+      if (e == cudaSuccess) e = launch_fan2para_quads(fan, par, batch, h->f2p->cfg(plane), st);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
+      if (e == cudaSuccess) e = launch_filter(par, batch, h->filt->cfg(), st);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[4], st);
+      if (e == cudaSuccess) {
+         BPCfg c = h->bp->cfg(fused);
+         c.mid_event = ev[5];
+         e = launch_backprojection(par, img, batch, c, h->bp->variant_for(batch, fused), st);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(ev[6], st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(ev[6]);
+      for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
+         float t = 0.f;
+         e = cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+         sum[k] += t;
+      }
+      if (e != cudaSuccess) rc = fail(RISA_GB_ECUDA, std::string("stage timing: ") + cudaGetErrorString(e));
+   }
+   for (auto& e : ev) cudaEventDestroy(e);
+   if (rc != RISA_GB_OK) return rc;
+   for (int k = 0; k < 6; ++k) ms[k] = (float)(sum[k] / reps);
+   return risa_gb_backprojection_check(h->bp);
 }
 
 // Captures the chunked reconstruction of n_frames frames on stream `st`.
@@ -1107,7 +1170,10 @@ struct risa_gb_toeplitz {
    Geometry g;
    Params p;
    int len = 0;
-   DevBuf th, tl, err;
+   DevBuf th, tl, err;        // bf16 split of T^T
+   DevBuf th16, tl16;         // fp16 split of T^T scaled by 1 / t_inv16
+   float t_inv16 = 1.0f;
+   int split = RISA_GB_SPLIT_BF16X3;
 };
 
 risa_gb_status risa_gb_toeplitz_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
@@ -1145,6 +1211,22 @@ risa_gb_status risa_gb_toeplitz_create(const risa_gb_geometry* gi, const risa_gb
       }
    RG_TRY(h->th.upload(th));
    RG_TRY(h->tl.upload(tl));
+   // fp16 split: T scaled by the power of two that puts max |c| in [2^13, 2^14)
+   double cmax = 0.0;
+   for (int d = 0; d < len; ++d) cmax = std::max(cmax, std::fabs(c[d]));
+   const int e = cmax > 0.0 ? std::ilogb(cmax) : 0;
+   const double ts = std::ldexp(1.0, 13 - e);
+   h->t_inv16 = (float)std::ldexp(1.0, e - 13);
+   std::vector<__half> t16h((size_t)Dp * Dp), t16l((size_t)Dp * Dp);
+   for (int n = 0; n < Dp; ++n)
+      for (int k = 0; k < Dp; ++k) {
+         const double v = c[((n - k) % len + len) % len] * ts;
+         const __half hi = __float2half_rn((float)v);
+         t16h[(size_t)n * Dp + k] = hi;
+         t16l[(size_t)n * Dp + k] = __float2half_rn((float)(v - (double)__half2float(hi)));
+      }
+   RG_TRY(h->th16.upload(t16h));
+   RG_TRY(h->tl16.upload(t16l));
    RG_TRY(h->err.alloc(sizeof(int)));
    RG_CUDA(cudaMemset(h->err.p, 0, sizeof(int)));
    *out = h.release();
@@ -1153,7 +1235,16 @@ risa_gb_status risa_gb_toeplitz_create(const risa_gb_geometry* gi, const risa_gb
 
 size_t risa_gb_toeplitz_workspace_bytes(const risa_gb_toeplitz* h, int batch) {
    if (!h || batch < 1) return 0;
-   return (size_t)2 * 2 * batch * h->g.Pp * h->g.Dp + 256;
+   const size_t n = ((size_t)batch * h->g.Pp * h->g.Dp + 127) & ~(size_t)127;
+   const size_t rows = (size_t)batch * h->g.Pp;
+   return 2 * 2 * n + sizeof(float) * rows + 256;  // hi, lo, row scales of the fp16 form
+}
+
+risa_gb_status risa_gb_toeplitz_set_precision(risa_gb_toeplitz* h, int split) {
+   if (!h || (split != RISA_GB_SPLIT_BF16X3 && split != RISA_GB_SPLIT_F16X3))
+      return fail(RISA_GB_EINVAL, "unknown split");
+   h->split = split;
+   return RISA_GB_OK;
 }
 
 risa_gb_status risa_gb_toeplitz_enqueue(risa_gb_toeplitz* h, float* sino, int batch, void* workspace,
@@ -1164,11 +1255,16 @@ risa_gb_status risa_gb_toeplitz_enqueue(risa_gb_toeplitz* h, float* sino, int ba
       return fail(RISA_GB_EINVAL, "workspace must be 256-byte and sino 16-byte aligned");
    ToeplitzArgs a;
    const size_t n = (size_t)batch * h->g.Pp * h->g.Dp;
+   const size_t n_al = (n + 127) & ~(size_t)127;
+   uint16_t* ws16 = static_cast<uint16_t*>(workspace);
    a.x = sino;
-   a.xh = static_cast<__nv_bfloat16*>(workspace);
-   a.xl = a.xh + ((n + 127) & ~(size_t)127);
-   a.th = h->th.as<__nv_bfloat16>();
-   a.tl = h->tl.as<__nv_bfloat16>();
+   a.xh = ws16;
+   a.xl = ws16 + n_al;
+   a.f16 = h->split == RISA_GB_SPLIT_F16X3 ? 1 : 0;
+   a.row_inv = reinterpret_cast<float*>(ws16 + 2 * n_al);
+   a.t_inv = a.f16 ? h->t_inv16 : 1.0f;
+   a.th = a.f16 ? h->th16.p : h->th.p;
+   a.tl = a.f16 ? h->tl16.p : h->tl.p;
    a.y = sino;
    a.rows = batch * h->g.Pp;
    a.n = h->g.Dp;

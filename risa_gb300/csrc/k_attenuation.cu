@@ -231,6 +231,74 @@ __global__ void logden_table(const float* __restrict__ avg, const float* __restr
    if (den < kClamp) den = kClamp;
    logden[(size_t)k * fs + i] = (float)log((double)den);
 }
+
+// ---- frame quads: the same rows of 4 frames of one plane per CTA -----------------
+// Rows of the quad's frames are staged in shared memory (128-bit loads), each
+// frame's defect runs are applied to its rows in list order, and every sample
+// position is attenuated for the 4 frames at once: one log(den) and dark read
+// for 4 outputs and one 16-byte store ([quad][P][D][4]).
+constexpr int kQRows = 4;
+
+__global__ void __launch_bounds__(kThreads) attenuation_quads(const uint16_t* __restrict__ raw,
+                                                              float4* __restrict__ fanq, AttenuationCfg cfg,
+                                                              QuadMap qm, const int* __restrict__ counts,
+                                                              const DefectRun* __restrict__ runs, int max_runs) {
+   extern __shared__ __align__(16) uint16_t tile[];  // [4][kQRows][D]
+   const int D = cfg.D, P = cfg.P;
+   const size_t fs = (size_t)P * D;
+   const int q = blockIdx.y;
+   const int k = quad_plane(qm, q);
+   const int y0 = blockIdx.x * kQRows;
+   const int rows = min(kQRows, P - y0);
+   const int n = rows * D;
+   int fr[4];
+#pragma unroll
+   for (int j = 0; j < 4; ++j) fr[j] = quad_frame(qm, q, j);
+   const bool vec = (D % 8) == 0 && (cfg.modules <= 0 || ((D / cfg.modules) % 8) == 0);
+#pragma unroll
+   for (int j = 0; j < 4; ++j) {
+      if (fr[j] < 0) continue;
+      const uint16_t* frame = raw + (size_t)fr[j] * fs;
+      uint16_t* t = tile + (size_t)j * kQRows * D;
+      if (vec) {
+         for (int i8 = threadIdx.x * 8; i8 < n; i8 += kThreads * 8) {
+            const int y = y0 + i8 / D, x = i8 % D;
+            *reinterpret_cast<uint4*>(t + i8) =
+                __ldg(reinterpret_cast<const uint4*>(frame + raw_offset(y, x, P, D, cfg.modules)));
+         }
+      } else {
+         for (int i = threadIdx.x; i < n; i += kThreads) t[i] = frame[raw_offset(y0 + i / D, i % D, P, D, cfg.modules)];
+      }
+   }
+   __syncthreads();
+   if (runs && threadIdx.x < 4 * kQRows) {
+      const int j = threadIdx.x / kQRows, r = threadIdx.x % kQRows;
+      const int fj = quad_frame(qm, q, j);
+      if (r < rows && fj >= 0) {
+         const int nr = counts[fj];
+         uint16_t* row = tile + ((size_t)j * kQRows + r) * D;
+         const DefectRun* rl = runs + (size_t)fj * max_runs;
+         for (int i = 0; i < nr; ++i) {
+            const DefectRun run = rl[i];
+            for (int m = 0; m < run.len; ++m) row[(run.start + m) % D] = repair_value(row, run, m, cfg.quirk);
+         }
+      }
+   }
+   __syncthreads();
+   const float* ld = cfg.logden + (size_t)k * fs + (size_t)y0 * D;
+   const float* dk = cfg.dark + (size_t)k * D;
+   float4* dst = fanq + ((size_t)q * P + y0) * D;
+   const size_t plane_stride = (size_t)kQRows * D;
+   for (int i = threadIdx.x; i < n; i += kThreads) {
+      const int x = i % D;
+      const float l = __ldg(ld + i), d = __ldg(dk + x);
+      float v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = fr[j] >= 0 ? atten_one(tile[j * plane_stride + i], d, l) : 0.f;
+      if (cfg.mask && !mask_keep(cfg.mask, cfg.wpr, y0 + i / D, x)) v[0] = v[1] = v[2] = v[3] = 0.f;
+      __stcs(dst + i, make_float4(v[0], v[1], v[2], v[3]));
+   }
+}
 }  // namespace
 
 cudaError_t launch_attenuation(const uint16_t* raw, float* out, int batch,
@@ -255,6 +323,22 @@ cudaError_t launch_attenuation(const uint16_t* raw, float* out, int batch,
       dim3 grid((unsigned)((fs + kThreads - 1) / kThreads), batch);
       attenuation_scalar<<<grid, kThreads, 0, st>>>(raw, out, cfg);
    }
+   return cudaGetLastError();
+}
+
+cudaError_t launch_attenuation_quads(const uint16_t* raw, float* fanq, int batch, const AttenuationCfg& cfg,
+                                     const DefectWorkspace* runs, int max_runs, cudaStream_t st) {
+   if (batch <= 0) return cudaSuccess;
+   const QuadMap qm = make_quad_map(cfg.L, cfg.plane, batch);
+   const size_t smem = sizeof(uint16_t) * 4 * kQRows * (size_t)cfg.D;
+   if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(attenuation_quads, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+   }
+   dim3 grid((cfg.P + kQRows - 1) / kQRows, quad_count(qm));
+   attenuation_quads<<<grid, kThreads, smem, st>>>(raw, reinterpret_cast<float4*>(fanq), cfg, qm,
+                                                   runs ? runs->counts : nullptr, runs ? runs->runs : nullptr,
+                                                   max_runs);
    return cudaGetLastError();
 }
 

@@ -704,43 +704,48 @@ cudaError_t launch_interp(const float* sino, float* img, int batch, const BPCfg&
 // |d| < 1). One thread per (angle, bin) walks the pixel rows (or columns,
 // whichever the ray crosses more steeply) and visits only the pixels whose
 // coordinate lies within one bin, so each output is a deterministic gather.
-__global__ void bp_adjoint(const float* __restrict__ img, float* __restrict__ sino, BPCfg cfg) {
+// No FP64 work in the loop: the line start t0 + y b (or t0 + x a) comes from
+// an FP64-built (hi, lo) float pair and the step from a (hi, lo) split of a
+// (or b), so t' - k = (hi - k + j step_hi) + (lo + j step_lo) keeps ~1e-7-bin
+// accuracy (hi - k is exact; the first sum is small where pixels are visited).
+__global__ void __launch_bounds__(128) bp_adjoint(const float* __restrict__ img, float* __restrict__ sino, BPCfg cfg) {
    const int k = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = blockIdx.y;
    const int slice = blockIdx.z;
    if (k >= cfg.Dp || i >= cfg.Pp) return;
    const int N = cfg.N;
-   const double a = cfg.ad[i], b = cfg.bd[i], t0 = cfg.t0[i];
+   const float a = __ldg(cfg.a + i), b = __ldg(cfg.b + i);
+   const bool along_x = fabsf(a) >= fabsf(b);  // walk x within rows
+   const float s_hi = along_x ? a : b;
+   const float s_lo = (float)((along_x ? __ldg(cfg.ad + i) : __ldg(cfg.bd + i)) - (double)s_hi);
+   const float inv = 1.0f / s_hi;  // |s_hi| >= scale / sqrt(2) > 0
+   const float2* line = (along_x ? cfg.rowbase : cfg.colbase) + (size_t)i * N;
    const float* im = img + (size_t)slice * N * N;
-   double acc = 0.0;
-   // t'(x, y) = t0 + x a + y b; contributions where |t' - k| < 1
-   if (fabs(a) >= fabs(b)) {
-      for (int y = 0; y < N; ++y) {
-         const double base = t0 + (double)y * b;
-         // x range with k - 1 < base + x a < k + 1
-         double xa = ((double)k - 1.0 - base) / a, xb = ((double)k + 1.0 - base) / a;
-         if (xa > xb) { const double t = xa; xa = xb; xb = t; }
-         int xs = max(0, (int)floor(xa)), xe = min(N - 1, (int)ceil(xb));
-         for (int x = xs; x <= xe; ++x) {
-            const float t = (float)(base + (double)x * a);
-            const float d = fabsf(t - (float)k);
-            if (d < 1.f) acc += (double)((1.f - d) * __ldg(im + (size_t)y * N + x));
-         }
+   const float kf = (float)k;
+   float acc0 = 0.f, acc1 = 0.f;
+   for (int r = 0; r < N; ++r) {
+      const float2 hb = __ldg(line + r);
+      const float t_hi = hb.x - kf, t_lo = hb.y;
+      const float t0 = t_hi + t_lo;
+      float ja = (-1.f - t0) * inv, jb = (1.f - t0) * inv;
+      if (ja > jb) {
+         const float tt = ja;
+         ja = jb;
+         jb = tt;
       }
-   } else {
-      for (int x = 0; x < N; ++x) {
-         const double base = t0 + (double)x * a;
-         double ya = ((double)k - 1.0 - base) / b, yb = ((double)k + 1.0 - base) / b;
-         if (ya > yb) { const double t = ya; ya = yb; yb = t; }
-         int ys = max(0, (int)floor(ya)), ye = min(N - 1, (int)ceil(yb));
-         for (int y = ys; y <= ye; ++y) {
-            const float t = (float)(base + (double)y * b);
-            const float d = fabsf(t - (float)k);
-            if (d < 1.f) acc += (double)((1.f - d) * __ldg(im + (size_t)y * N + x));
+      if (jb < -1.f || ja > (float)N) continue;
+      const int js = max(0, (int)floorf(ja) - 1), je = min(N - 1, (int)ceilf(jb) + 1);
+      for (int j = js; j <= je; ++j) {
+         const float jf = (float)j;
+         const float d = fabsf(fmaf(jf, s_hi, t_hi) + fmaf(jf, s_lo, t_lo));
+         if (d < 1.f) {
+            const float v = along_x ? __ldg(im + (size_t)r * N + j) : __ldg(im + (size_t)j * N + r);
+            if (j & 1) acc1 = fmaf(1.f - d, v, acc1);
+            else acc0 = fmaf(1.f - d, v, acc0);
          }
       }
    }
-   sino[((size_t)slice * cfg.Pp + i) * cfg.Dp + k] = (float)acc * cfg.norm;
+   sino[((size_t)slice * cfg.Pp + i) * cfg.Dp + k] = (acc0 + acc1) * cfg.norm;
 }
 }  // namespace
 
@@ -789,6 +794,17 @@ void bp_window_extent(const float* a, const float* b, const double* ad, const do
    *win_len = (int)(hi - lo + 4);
 }
 
+std::vector<float2> bp_line_starts(const double* t0, const double* step, int Pp, int N) {
+   std::vector<float2> out((size_t)Pp * N);
+   for (int i = 0; i < Pp; ++i)
+      for (int j = 0; j < N; ++j) {
+         const double v = t0[i] + (double)j * step[i];
+         const float hi = (float)v;
+         out[(size_t)i * N + j] = make_float2(hi, (float)(v - (double)hi));
+      }
+   return out;
+}
+
 cudaError_t launch_backprojection(const float* sino, float* img, int batch, const BPCfg& cfg,
                                   int variant, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
@@ -828,6 +844,7 @@ cudaError_t launch_backprojection(const float* sino, float* img, int batch, cons
 cudaError_t launch_backprojection_adjoint(const float* img, float* sino, int batch,
                                           const BPCfg& cfg, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
+   if (!cfg.rowbase || !cfg.colbase) return cudaErrorInvalidValue;
    dim3 grid((cfg.Dp + 127) / 128, cfg.Pp, batch);
    bp_adjoint<<<grid, 128, 0, st>>>(img, sino, cfg);
    return cudaGetLastError();

@@ -115,26 +115,30 @@ __global__ void __launch_bounds__(kThreads) filter_rows(float* __restrict__ sino
 __global__ void __launch_bounds__(kThreads) filter_grad_partial(const float* __restrict__ x,
                                                                 const float* __restrict__ g,
                                                                 int total_rows, FilterCfg cfg, int tpp,
-                                                                float2* __restrict__ partial) {
+                                                                float2* __restrict__ partial, int groups) {
    extern __shared__ float2 buf[];
    const int len = cfg.len;
    const int ppb = kThreads / tpp;
    const int local = threadIdx.x / tpp, lt = threadIdx.x % tpp;
-   const int pair = blockIdx.x * ppb + local;
-   const int ra = 2 * pair, rb = 2 * pair + 1;
-   const bool has_a = ra < total_rows, has_b = rb < total_rows;
    float2* bx0 = buf + (size_t)local * 4 * len;
    float2* bx1 = bx0 + len;
    float2* bg0 = bx1 + len;
    float2* bg1 = bg0 + len;
    float2* acc = buf + (size_t)ppb * 4 * len;  // [len], shared by the CTA's pairs
    const int Dp = cfg.Dp;
+   for (int k = threadIdx.x; k < len; k += kThreads) acc[k] = make_float2(0.f, 0.f);
+   // groups of ppb row pairs, a fixed grid-stride assignment (the sum order
+   // depends only on the grid size, which the launcher fixes)
+   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+   const int pair = grp * ppb + local;
+   const int ra = 2 * pair, rb = 2 * pair + 1;
+   const bool has_a = ra < total_rows, has_b = rb < total_rows;
+   __syncthreads();  // the previous group's transforms are done with the buffers
    for (int n = lt; n < len; n += tpp) {
       const bool in = n < Dp;
       bx0[n] = make_float2((has_a && in) ? x[(size_t)ra * Dp + n] : 0.f, (has_b && in) ? x[(size_t)rb * Dp + n] : 0.f);
       bg0[n] = make_float2((has_a && in) ? g[(size_t)ra * Dp + n] : 0.f, (has_b && in) ? g[(size_t)rb * Dp + n] : 0.f);
    }
-   for (int k = threadIdx.x; k < len; k += kThreads) acc[k] = make_float2(0.f, 0.f);
    __syncthreads();
    float2* zx = fft(bx0, bx1, cfg.twiddle, len, lt, tpp);
    float2* zg = fft(bg0, bg1, cfg.twiddle, len, lt, tpp);
@@ -157,7 +161,23 @@ __global__ void __launch_bounds__(kThreads) filter_grad_partial(const float* __r
       }
       __syncthreads();
    }
+   }
    for (int k = threadIdx.x; k < len; k += kThreads) partial[(size_t)blockIdx.x * len + k] = acc[k];
+}
+
+// Sum of the partial spectra in block order, one frequency per thread;
+// spec receives the conjugate (the finish kernel inverts by conj(FFT(conj))).
+__global__ void __launch_bounds__(kThreads) filter_grad_sum(const float2* __restrict__ partial, int blocks, int len,
+                                                            float2* __restrict__ spec) {
+   const int k = blockIdx.x * kThreads + threadIdx.x;
+   if (k >= len) return;
+   float sx = 0.f, sy = 0.f;
+   for (int j = 0; j < blocks; ++j) {
+      const float2 v = partial[(size_t)j * len + k];
+      sx += v.x;
+      sy += v.y;
+   }
+   spec[k] = make_float2(sx, -sy);
 }
 
 
@@ -210,23 +230,14 @@ cudaError_t launch_r16(float* sino, int total_rows, const FilterCfg& cfg, cudaSt
    return cudaGetLastError();
 }
 
-// One CTA: sum the partial spectra in block order, invert, scale by 1/len.
-__global__ void __launch_bounds__(kThreads) filter_grad_finish(const float2* __restrict__ partial,
-                                                               int blocks, FilterCfg cfg, int n_taps,
-                                                               int center, float* __restrict__ grad) {
+// One CTA: invert the summed (conjugated) spectrum, scale by 1/len, map lags to taps.
+__global__ void __launch_bounds__(kThreads) filter_grad_finish(const float2* __restrict__ spec, FilterCfg cfg,
+                                                               int n_taps, int center, float* __restrict__ grad) {
    extern __shared__ float2 buf[];
    const int len = cfg.len;
    float2* a = buf;
    float2* b = buf + len;
-   for (int k = threadIdx.x; k < len; k += kThreads) {
-      float2 s = make_float2(0.f, 0.f);
-      for (int j = 0; j < blocks; ++j) {
-         const float2 v = partial[(size_t)j * len + k];
-         s.x += v.x;
-         s.y += v.y;
-      }
-      a[k] = make_float2(s.x, -s.y);  // conj for the inverse
-   }
+   for (int k = threadIdx.x; k < len; k += kThreads) a[k] = spec[k];
    __syncthreads();
    // one transform spread over the first tpp threads; the others only meet the barriers
    const int tpp = len / 8 < kThreads ? len / 8 : kThreads;
@@ -237,34 +248,45 @@ __global__ void __launch_bounds__(kThreads) filter_grad_finish(const float2* __r
 }
 }  // namespace
 
+// Grid of the partial-spectrum kernel: at most kGradBlocks CTAs, each
+// accumulating a fixed set of row-pair groups.
+constexpr int kGradBlocks = 512;
+struct GradPlan {
+   int tpp, ppb, groups, blocks;
+};
+static GradPlan grad_plan(const FilterCfg& cfg, int batch) {
+   GradPlan g;
+   g.tpp = cfg.len / 8 < kThreads ? cfg.len / 8 : kThreads;
+   g.ppb = kThreads / g.tpp;
+   const int pairs = (batch * cfg.rows + 1) / 2;
+   g.groups = (pairs + g.ppb - 1) / g.ppb;
+   g.blocks = g.groups < kGradBlocks ? g.groups : kGradBlocks;
+   return g;
+}
+
 size_t filter_grad_workspace_bytes(const FilterCfg& cfg, int batch) {
-   const int total_rows = batch * cfg.rows;
-   const int tpp = cfg.len / 8 < kThreads ? cfg.len / 8 : kThreads;
-   const int ppb = kThreads / tpp;
-   const int pairs = (total_rows + 1) / 2;
-   const int blocks = (pairs + ppb - 1) / ppb;
-   return sizeof(float2) * (size_t)cfg.len * blocks;
+   const GradPlan g = grad_plan(cfg, batch);
+   return sizeof(float2) * (size_t)cfg.len * (g.blocks + 1);  // partial spectra + their sum
 }
 
 cudaError_t launch_filter_taps_grad(const float* x, const float* g, int batch, const FilterCfg& cfg,
                                     float2* workspace, int n_taps, int center, float* grad_taps,
                                     cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
-   const int total_rows = batch * cfg.rows;
-   const int tpp = cfg.len / 8 < kThreads ? cfg.len / 8 : kThreads;
-   const int ppb = kThreads / tpp;
-   const int pairs = (total_rows + 1) / 2;
-   const int blocks = (pairs + ppb - 1) / ppb;
-   const size_t smem = sizeof(float2) * ((size_t)4 * cfg.len * ppb + cfg.len);
+   const GradPlan gp = grad_plan(cfg, batch);
+   const size_t smem = sizeof(float2) * ((size_t)4 * cfg.len * gp.ppb + cfg.len);
    if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
    cudaError_t e = cudaFuncSetAttribute(filter_grad_partial, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem);
    if (e != cudaSuccess) return e;
-   filter_grad_partial<<<blocks, kThreads, smem, st>>>(x, g, total_rows, cfg, tpp, workspace);
+   filter_grad_partial<<<gp.blocks, kThreads, smem, st>>>(x, g, batch * cfg.rows, cfg, gp.tpp, workspace,
+                                                          gp.groups);
+   float2* spec = workspace + (size_t)gp.blocks * cfg.len;
+   filter_grad_sum<<<(cfg.len + kThreads - 1) / kThreads, kThreads, 0, st>>>(workspace, gp.blocks, cfg.len, spec);
    const size_t smem2 = sizeof(float2) * 2 * (size_t)cfg.len;
    e = cudaFuncSetAttribute(filter_grad_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
    if (e != cudaSuccess) return e;
-   filter_grad_finish<<<1, kThreads, smem2, st>>>(workspace, blocks, cfg, n_taps, center, grad_taps);
+   filter_grad_finish<<<1, kThreads, smem2, st>>>(spec, cfg, n_taps, center, grad_taps);
    return cudaGetLastError();
 }
 

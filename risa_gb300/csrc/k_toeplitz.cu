@@ -25,6 +25,7 @@
 // frees its tensor memory before returning.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -68,16 +69,19 @@ __device__ __forceinline__ uint64_t smem_desc(const void* tile) {
    return d;
 }
 
-// Instruction descriptor, kind::f16: bf16 A and B, f32 D, both K-major, M128 N128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
-                            ((uint32_t)(kBM >> 4) << 24);
+// Instruction descriptors, kind::f16, f32 D, both operands K-major, M128 N128:
+// A and B both bf16, or both fp16 (never mixed).
+constexpr uint32_t kIdescBf16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
+                                ((uint32_t)(kBM >> 4) << 24);
+constexpr uint32_t kIdescF16 = (1u << 4) | ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
 
-__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
    asm volatile(
        "{\n\t.reg .pred p;\n\t"
        "setp.ne.b32 p, %4, 0;\n\t"
        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-       "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
        : "memory");
 }
 
@@ -106,7 +110,8 @@ __global__ void __launch_bounds__(128, 1) toeplitz_gemm(const __grid_constant__ 
                                                         const __grid_constant__ CUtensorMap map_th,
                                                         const __grid_constant__ CUtensorMap map_tl,
                                                         float* __restrict__ y, int M, int N, int K,
-                                                        int* __restrict__ err) {
+                                                        int* __restrict__ err, uint32_t idesc,
+                                                        const float* __restrict__ row_inv, float t_inv) {
    extern __shared__ __align__(1024) unsigned char smem_raw[];
    // stages must sit on 1024-byte boundaries for the 128-byte swizzle
    unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -173,9 +178,9 @@ __global__ void __launch_bounds__(128, 1) toeplitz_gemm(const __grid_constant__ 
                // advance 16 bf16 (32 bytes) along K inside the swizzle atom
                const uint64_t o = (uint64_t)((kk * 32) >> 4);
                const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
-               umma_f16(tmem_d, dxh + o, dth + o, acc0);
-               umma_f16(tmem_d, dxh + o, dtl + o, 1u);
-               umma_f16(tmem_d, dxl + o, dth + o, 1u);
+               umma_f16(tmem_d, dxh + o, dth + o, idesc, acc0);
+               umma_f16(tmem_d, dxh + o, dtl + o, idesc, 1u);
+               umma_f16(tmem_d, dxl + o, dth + o, idesc, 1u);
             }
             umma_commit(&empty_bar[s]);  // the stage is free once these MMAs finish
          }
@@ -195,10 +200,12 @@ __global__ void __launch_bounds__(128, 1) toeplitz_gemm(const __grid_constant__ 
          tmem_ld32(tmem_d + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
          if (row < M) {
             float4* dst = reinterpret_cast<float4*>(y + (size_t)row * N + n0 + c);
+            // power-of-two scales of the fp16 form: exact
+            const float sc = row_inv ? row_inv[row] * t_inv : t_inv;
 #pragma unroll
             for (int q = 0; q < 8; ++q)
-               dst[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
-                                    __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+               dst[q] = make_float4(__uint_as_float(r[4 * q]) * sc, __uint_as_float(r[4 * q + 1]) * sc,
+                                    __uint_as_float(r[4 * q + 2]) * sc, __uint_as_float(r[4 * q + 3]) * sc);
          }
       }
    }
@@ -221,6 +228,29 @@ __global__ void split_bf16(const float* __restrict__ x, __nv_bfloat16* __restric
    lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
+// fp32 rows -> scaled fp16 (hi, lo): one warp per row; the row is scaled by the
+// power of two s that puts its largest magnitude in [2^13, 2^14) (exact), hi =
+// rn(x s), lo = rn(x s - hi); row_inv = 1 / s.
+__global__ void split_f16_rows(const float* __restrict__ x, __half* __restrict__ hi, __half* __restrict__ lo,
+                               float* __restrict__ row_inv, int rows, int k) {
+   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
+   if (row >= rows) return;
+   const float* xr = x + (size_t)row * k;
+   float m = 0.f;
+   for (int j = lane; j < k; j += 32) m = fmaxf(m, fabsf(xr[j]));
+#pragma unroll
+   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+   const int e = m > 0.f ? ilogbf(m) : 0;
+   const float s = ldexpf(1.0f, 13 - e), inv = ldexpf(1.0f, e - 13);
+   for (int j = lane; j < k; j += 32) {
+      const float v = xr[j] * s;
+      const __half h = __float2half_rn(v);
+      hi[(size_t)row * k + j] = h;
+      lo[(size_t)row * k + j] = __float2half_rn(v - __half2float(h));
+   }
+   if (lane == 0) row_inv[row] = inv;
+}
+
 using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -237,15 +267,15 @@ EncodeTiled encode_fn() {
    return fn;
 }
 
-// bf16 matrix [rows][cols] (cols contiguous), boxes of 64 columns x 128 rows.
-bool make_map(CUtensorMap* map, const void* base, int rows, int cols) {
+// 16-bit matrix [rows][cols] (cols contiguous), boxes of 64 columns x 128 rows.
+bool make_map(CUtensorMap* map, const void* base, int rows, int cols, bool f16) {
    EncodeTiled enc = encode_fn();
    if (!enc) return false;
    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
    const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
    const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
    const cuuint32_t estr[2] = {1, 1};
-   return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+   return enc(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -257,16 +287,25 @@ cudaError_t launch_toeplitz(const ToeplitzArgs& a, cudaStream_t st) {
    if (a.rows <= 0) return cudaSuccess;
    if (a.n % kBN || a.k % kBK) return cudaErrorInvalidValue;
    const size_t n = (size_t)a.rows * a.k;
-   split_bf16<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a.x, a.xh, a.xl, n);
+   const bool f16 = a.f16 != 0;
+   if (f16) {
+      if (!a.row_inv) return cudaErrorInvalidValue;
+      split_f16_rows<<<(a.rows + 7) / 8, 256, 0, st>>>(a.x, static_cast<__half*>(a.xh), static_cast<__half*>(a.xl),
+                                                       a.row_inv, a.rows, a.k);
+   } else {
+      split_bf16<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a.x, static_cast<__nv_bfloat16*>(a.xh),
+                                                             static_cast<__nv_bfloat16*>(a.xl), n);
+   }
    CUtensorMap mxh, mxl, mth, mtl;
-   if (!make_map(&mxh, a.xh, a.rows, a.k) || !make_map(&mxl, a.xl, a.rows, a.k) ||
-       !make_map(&mth, a.th, a.n, a.k) || !make_map(&mtl, a.tl, a.n, a.k))
+   if (!make_map(&mxh, a.xh, a.rows, a.k, f16) || !make_map(&mxl, a.xl, a.rows, a.k, f16) ||
+       !make_map(&mth, a.th, a.n, a.k, f16) || !make_map(&mtl, a.tl, a.n, a.k, f16))
       return cudaErrorInvalidValue;
    const size_t smem = toeplitz_smem_bytes();
    cudaError_t e = cudaFuncSetAttribute(toeplitz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
    if (e != cudaSuccess) return e;
    dim3 grid(a.n / kBN, (a.rows + kBM - 1) / kBM);
-   toeplitz_gemm<<<grid, 128, smem, st>>>(mxh, mxl, mth, mtl, a.y, a.rows, a.n, a.k, a.err);
+   toeplitz_gemm<<<grid, 128, smem, st>>>(mxh, mxl, mth, mtl, a.y, a.rows, a.n, a.k, a.err,
+                                          f16 ? kIdescF16 : kIdescBf16, f16 ? a.row_inv : nullptr, a.t_inv);
    return cudaGetLastError();
 }
 

@@ -103,6 +103,35 @@ cudaError_t launch_dark_average(const uint16_t* frames, int n_frames, int L, int
 cudaError_t launch_logden(const float* avg, const float* dark, int L, int P, int D,
                           float* logden, cudaStream_t st);
 
+// Frame quads: the engine keeps attenuated fan frames as [quad][P][D][4] float,
+// 4 frames of one plane side by side, so the per-sample work of the 4 frames
+// shares its table reads and moves 16 bytes at a time. Quad q holds frames of
+// plane quad_plane(q); lane j is frame quad_frame(q, j) of the batch, or -1.
+struct QuadMap {
+   int L, plane, batch, per_plane;  // per_plane: quads per plane
+};
+__host__ __device__ inline QuadMap make_quad_map(int L, int plane, int batch) {
+   QuadMap m;
+   m.L = plane >= 0 ? 1 : L;
+   m.plane = plane;
+   m.batch = batch;
+   const int most = (batch + m.L - 1) / m.L;  // frames of the fullest plane
+   m.per_plane = (most + 3) / 4;
+   return m;
+}
+__host__ __device__ inline int quad_count(const QuadMap& m) { return m.L * m.per_plane; }
+__host__ __device__ inline int quad_plane(const QuadMap& m, int q) {
+   return m.plane >= 0 ? m.plane : q / m.per_plane;
+}
+__host__ __device__ inline int quad_frame(const QuadMap& m, int q, int j) {
+   const int i = 4 * (q % m.per_plane) + j;  // index among the frames of the plane
+   const int b = m.plane >= 0 ? i : q / m.per_plane + m.L * i;
+   return b < m.batch ? b : -1;
+}
+// Attenuation (+ fused defect repair) of a batch into frame quads.
+cudaError_t launch_attenuation_quads(const uint16_t* raw, float* fanq, int batch, const AttenuationCfg& cfg,
+                                     const DefectWorkspace* runs, int max_runs, cudaStream_t st);
+
 // ---------------------------------------------------------------- fan2para
 struct F2PCfg {
    int Pf, Df, Pp, Dp, L;
@@ -113,6 +142,9 @@ struct F2PCfg {
 };
 cudaError_t launch_fan2para(const float* fan, float* par, int batch, const F2PCfg& cfg,
                             cudaStream_t st);
+// Rebinning from frame quads (see QuadMap) into per-frame parallel sinograms.
+cudaError_t launch_fan2para_quads(const float* fanq, float* par, int batch, const F2PCfg& cfg,
+                                  cudaStream_t st);
 // Transpose of the rebinning through a CSR table over fan samples.
 struct F2PAdjCfg {
    int Pf, Df, Pp, Dp, L;
@@ -169,7 +201,13 @@ struct BPCfg {
    // host side only: recorded on the stream after the staging pass and before
    // the backprojection kernel (timing of the two separately)
    cudaEvent_t mid_event = nullptr;
+   // adjoint: FP64 line starts split as (hi, lo) floats, [Pp][N]:
+   // rowbase = t0 + y * b (walks along x), colbase = t0 + x * a (walks along y)
+   const float2* rowbase = nullptr;
+   const float2* colbase = nullptr;
 };
+// (hi, lo) float pairs of t0[i] + j * step[i], j < N, for every angle i.
+std::vector<float2> bp_line_starts(const double* t0, const double* step, int Pp, int N);
 int bp_variant_count();
 const char* bp_variant_name(int v);
 // Device bytes of the pair sinogram that `variant` needs for `batch` slices
