@@ -25,9 +25,63 @@
 #include <vector>
 
 #include "../glados_gb/Image.h"
+#include "Packets.h"
 #include "Stages.h"
 
 namespace risa_gb {
+
+// Packet layout of the detector modules from the configuration keys the
+// reference's receiver reads (ReceiverModule.cpp:139-163).
+inline PacketLayout packet_layout(const Config& cfg) {
+   PacketLayout L;
+   L.modules = cfg.geometry.n_modules;
+   L.det_per_module = (int)cfg.integer("numberOfDetectorsPerModule",
+                                       L.modules > 0 ? cfg.geometry.n_fan_det / L.modules : 0);
+   L.proj = cfg.geometry.n_fan_proj;
+   L.proj_per_packet = (int)cfg.integer("numberOfProjectionsPerPacket", L.proj);
+   L.ring = (int)cfg.integer("inputBufferSize", 32);
+   return L;
+}
+
+// Source stage of the online mode: the reference's Receiver::loadImage
+// (Receiver.cpp:66-86) over a FrameAssembler fed by any transport. Each
+// complete frame is copied from the ring into a pooled module-major image
+// (the OfflineLoader's output layout) and released; the stream ends (invalid
+// image) when the assembler finishes or no frame completes within `timeout`
+// seconds (config key timeout, as the reference's receiver modules).
+class OnlineLoader {
+ public:
+   using manager_type = cuda::RawHostManager;
+   using output_type = glados_gb::Image<manager_type>;
+
+   OnlineLoader(const std::string& config_file, FrameAssembler& frames) : cfg_(config_file), fa_(frames) {
+      const PacketLayout& L = fa_.layout();
+      if (L.frame_values() != (size_t)cfg_.geometry.n_fan_proj * cfg_.geometry.n_fan_det)
+         throw std::runtime_error("OnlineLoader: packet layout does not match the geometry");
+      timeout_ = (double)cfg_.integer("timeout", 10);
+      pool_ = glados_gb::MemoryPool<manager_type>::instance()->registerStage(8, L.frame_values());
+   }
+   ~OnlineLoader() { glados_gb::MemoryPool<manager_type>::instance()->freeMemory(pool_); }
+
+   output_type loadImage() {
+      uint64_t index = 0;
+      const uint16_t* frame = nullptr;
+      if (!fa_.next(&index, &frame, timeout_)) return output_type();
+      output_type img = glados_gb::MemoryPool<manager_type>::instance()->requestMemory(pool_);
+      std::copy(frame, frame + fa_.layout().frame_values(), img.data());
+      fa_.release(index);
+      img.setIdx((size_t)index);
+      img.setPlane((size_t)(index % (uint64_t)cfg_.geometry.n_planes));
+      img.setStart(std::chrono::high_resolution_clock::now());
+      return img;
+   }
+
+ private:
+   Config cfg_;
+   FrameAssembler& fa_;
+   double timeout_ = 10.0;
+   int pool_ = 0;
+};
 
 class OfflineLoader {
  public:

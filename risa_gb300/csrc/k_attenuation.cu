@@ -271,16 +271,30 @@ __global__ void __launch_bounds__(kThreads) attenuation_quads(const uint16_t* __
       }
    }
    __syncthreads();
-   if (runs && threadIdx.x < 4 * kQRows) {
-      const int j = threadIdx.x / kQRows, r = threadIdx.x % kQRows;
-      const int fj = quad_frame(qm, q, j);
-      if (r < rows && fj >= 0) {
+   if (runs) {
+      // one warp per (frame, row) of the tile; NONE-mode runs are independent
+      // (each is repaired from good columns only), so lanes take runs in
+      // parallel; RISA-mode runs are applied in list order by one lane, as the
+      // reference's loop does
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int jr = warp; jr < 4 * kQRows; jr += kThreads / 32) {
+         const int j = jr / kQRows, r = jr % kQRows;
+         const int fj = quad_frame(qm, q, j);
+         if (r >= rows || fj < 0) continue;
          const int nr = counts[fj];
          uint16_t* row = tile + ((size_t)j * kQRows + r) * D;
          const DefectRun* rl = runs + (size_t)fj * max_runs;
-         for (int i = 0; i < nr; ++i) {
-            const DefectRun run = rl[i];
-            for (int m = 0; m < run.len; ++m) row[(run.start + m) % D] = repair_value(row, run, m, cfg.quirk);
+         if (cfg.quirk == RISA_GB_QUIRKS_RISA) {
+            if (lane == 0)
+               for (int i = 0; i < nr; ++i) {
+                  const DefectRun run = rl[i];
+                  for (int m = 0; m < run.len; ++m) row[(run.start + m) % D] = repair_value(row, run, m, cfg.quirk);
+               }
+         } else {
+            for (int i = lane; i < nr; i += 32) {
+               const DefectRun run = rl[i];
+               for (int m = 0; m < run.len; ++m) row[(run.start + m) % D] = repair_value(row, run, m, cfg.quirk);
+            }
          }
       }
    }

@@ -708,23 +708,31 @@ cudaError_t launch_interp(const float* sino, float* img, int batch, const BPCfg&
 // an FP64-built (hi, lo) float pair and the step from a (hi, lo) split of a
 // (or b), so t' - k = (hi - k + j step_hi) + (lo + j step_lo) keeps ~1e-7-bin
 // accuracy (hi - k is exact; the first sum is small where pixels are visited).
-__global__ void __launch_bounds__(128) bp_adjoint(const float* __restrict__ img, float* __restrict__ sino, BPCfg cfg) {
+template <int SB>
+__global__ void __launch_bounds__(128) bp_adjoint(const float* __restrict__ img, float* __restrict__ sino, BPCfg cfg,
+                                                  int batch) {
+   extern __shared__ float2 s_line[];  // this angle's line starts [N]
    const int k = blockIdx.x * blockDim.x + threadIdx.x;
    const int i = blockIdx.y;
-   const int slice = blockIdx.z;
-   if (k >= cfg.Dp || i >= cfg.Pp) return;
+   const int s0 = blockIdx.z * SB;
    const int N = cfg.N;
    const float a = __ldg(cfg.a + i), b = __ldg(cfg.b + i);
    const bool along_x = fabsf(a) >= fabsf(b);  // walk x within rows
+   const float2* line = (along_x ? cfg.rowbase : cfg.colbase) + (size_t)i * N;
+   for (int r = threadIdx.x; r < N; r += blockDim.x) s_line[r] = __ldg(line + r);
+   __syncthreads();
+   if (k >= cfg.Dp) return;
    const float s_hi = along_x ? a : b;
    const float s_lo = (float)((along_x ? __ldg(cfg.ad + i) : __ldg(cfg.bd + i)) - (double)s_hi);
    const float inv = 1.0f / s_hi;  // |s_hi| >= scale / sqrt(2) > 0
-   const float2* line = (along_x ? cfg.rowbase : cfg.colbase) + (size_t)i * N;
-   const float* im = img + (size_t)slice * N * N;
+   const size_t plane = (size_t)N * N;
+   const float* im = img + (size_t)s0 * plane;
    const float kf = (float)k;
-   float acc0 = 0.f, acc1 = 0.f;
+   float acc[SB];
+#pragma unroll
+   for (int s = 0; s < SB; ++s) acc[s] = 0.f;
    for (int r = 0; r < N; ++r) {
-      const float2 hb = __ldg(line + r);
+      const float2 hb = s_line[r];
       const float t_hi = hb.x - kf, t_lo = hb.y;
       const float t0 = t_hi + t_lo;
       float ja = (-1.f - t0) * inv, jb = (1.f - t0) * inv;
@@ -739,13 +747,17 @@ __global__ void __launch_bounds__(128) bp_adjoint(const float* __restrict__ img,
          const float jf = (float)j;
          const float d = fabsf(fmaf(jf, s_hi, t_hi) + fmaf(jf, s_lo, t_lo));
          if (d < 1.f) {
-            const float v = along_x ? __ldg(im + (size_t)r * N + j) : __ldg(im + (size_t)j * N + r);
-            if (j & 1) acc1 = fmaf(1.f - d, v, acc1);
-            else acc0 = fmaf(1.f - d, v, acc0);
+            const float w = 1.f - d;
+            const size_t off = along_x ? (size_t)r * N + j : (size_t)j * N + r;
+#pragma unroll
+            for (int s = 0; s < SB; ++s)
+               if (s0 + s < batch) acc[s] = fmaf(w, __ldg(im + (size_t)s * plane + off), acc[s]);
          }
       }
    }
-   sino[((size_t)slice * cfg.Pp + i) * cfg.Dp + k] = (acc0 + acc1) * cfg.norm;
+#pragma unroll
+   for (int s = 0; s < SB; ++s)
+      if (s0 + s < batch) sino[((size_t)(s0 + s) * cfg.Pp + i) * cfg.Dp + k] = acc[s] * cfg.norm;
 }
 }  // namespace
 
@@ -845,8 +857,16 @@ cudaError_t launch_backprojection_adjoint(const float* img, float* sino, int bat
                                           const BPCfg& cfg, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
    if (!cfg.rowbase || !cfg.colbase) return cudaErrorInvalidValue;
-   dim3 grid((cfg.Dp + 127) / 128, cfg.Pp, batch);
-   bp_adjoint<<<grid, 128, 0, st>>>(img, sino, cfg);
+   // slices share the geometry: each thread applies its weights to SB slices
+   const size_t smem = sizeof(float2) * (size_t)cfg.N;
+   if (smem > 48 * 1024) return cudaErrorInvalidConfiguration;  // N <= 6144
+   if (batch >= 8) {
+      dim3 grid((cfg.Dp + 127) / 128, cfg.Pp, (batch + 7) / 8);
+      bp_adjoint<8><<<grid, 128, smem, st>>>(img, sino, cfg, batch);
+   } else {
+      dim3 grid((cfg.Dp + 127) / 128, cfg.Pp, batch);
+      bp_adjoint<1><<<grid, 128, smem, st>>>(img, sino, cfg, batch);
+   }
    return cudaGetLastError();
 }
 
