@@ -23,10 +23,13 @@ __device__ __forceinline__ int frame_plane(int b, int plane, int L) {
    return plane >= 0 ? plane : (b % L);
 }
 
+// log(den) - log(num) with log(num) from the hardware logarithm, as the
+// reference's -log(num/den) is compiled (-use_fast_math: log -> __logf);
+// its error (at most a few ulp of log(num)) is far below the FP32 bar.
 __device__ __forceinline__ float atten_one(unsigned raw, float dark, float logden) {
    float num = __fsub_rn((float)raw, dark);
    if (num < kClamp) num = kClamp;
-   return __fsub_rn(logden, logf(num));
+   return __fsub_rn(logden, __logf(num));
 }
 
 __device__ __forceinline__ bool mask_keep(const uint32_t* mask, int wpr, int y, int x) {
@@ -299,18 +302,20 @@ __global__ void __launch_bounds__(kThreads) attenuation_quads(const uint16_t* __
       }
    }
    __syncthreads();
-   const float* ld = cfg.logden + (size_t)k * fs + (size_t)y0 * D;
    const float* dk = cfg.dark + (size_t)k * D;
-   float4* dst = fanq + ((size_t)q * P + y0) * D;
    const size_t plane_stride = (size_t)kQRows * D;
-   for (int i = threadIdx.x; i < n; i += kThreads) {
-      const int x = i % D;
-      const float l = __ldg(ld + i), d = __ldg(dk + x);
-      float v[4];
+   for (int r = 0; r < rows; ++r) {  // row by row: no index division per sample
+      const float* ld = cfg.logden + (size_t)k * fs + (size_t)(y0 + r) * D;
+      float4* dst = fanq + ((size_t)q * P + y0 + r) * D;
+      const uint16_t* t = tile + (size_t)r * D;
+      for (int x = threadIdx.x; x < D; x += kThreads) {
+         const float l = __ldg(ld + x), d = __ldg(dk + x);
+         float v[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) v[j] = fr[j] >= 0 ? atten_one(tile[j * plane_stride + i], d, l) : 0.f;
-      if (cfg.mask && !mask_keep(cfg.mask, cfg.wpr, y0 + i / D, x)) v[0] = v[1] = v[2] = v[3] = 0.f;
-      __stcs(dst + i, make_float4(v[0], v[1], v[2], v[3]));
+         for (int j = 0; j < 4; ++j) v[j] = fr[j] >= 0 ? atten_one(t[j * plane_stride + x], d, l) : 0.f;
+         if (cfg.mask && !mask_keep(cfg.mask, cfg.wpr, y0 + r, x)) v[0] = v[1] = v[2] = v[3] = 0.f;
+         __stcs(dst + x, make_float4(v[0], v[1], v[2], v[3]));
+      }
    }
 }
 }  // namespace
