@@ -313,7 +313,10 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     fs, ps = Pf * Df, Pp * Dp
     att_bytes = B * fs * (2 + 4) + L * fs * 4
     f2p_bytes = B * (fs * 4 + ps * 4) + L * ps * 4 * 12
-    filt_bytes = B * ps * 8
+    # the filter reads the rebinned sinogram; fused with the staging pass it
+    # writes the padded pair records (8 B per window bin, angle and slice)
+    win_lo, win_len = bp.window(True)
+    filt_bytes = B * ps * 4 + (B * Pp * win_len * 8 if t_stage < 1e-3 else B * ps * 4)
     yy, xx = np.mgrid[:N, :N]
     inside = int(((xx - (N - 1) / 2) ** 2 + (yy - (N - 1) / 2) ** 2 <= N * N / 4).sum())
     updates = B * inside * Pp
@@ -511,6 +514,7 @@ def measure_differentiation(torch, rg, dev):
     filt = rg.Filter(g, p, taps=taps)
     bp = rg.Backprojection(g, p)
     bp.reserve(S)
+    bp.reserve_adjoint(S)
     s = torch.from_numpy(rng.standard_normal((S, Pp, Dp)).astype(np.float32)).to(dev)
     y = torch.from_numpy(rng.standard_normal((S, N, N)).astype(np.float32)).to(dev)
     fs, img = torch.empty_like(s), torch.empty((S, N, N), dtype=torch.float32, device=dev)

@@ -306,6 +306,19 @@ risa_gb_status risa_gb_backprojection_reserve(risa_gb_backprojection* h, int max
 risa_gb_status risa_gb_backprojection_time(risa_gb_backprojection* h, const float* sino, float* img,
                                            int batch, int reps, void* stream, float* staging_ms,
                                            float* kernel_ms);
+/* Allocates the adjoint's scratch (two slice-interleaved copies of the image,
+ * one transposed, 8 N^2 floats per group of 8 slices) for batches up to
+ * max_batch. Set-up call: may allocate and synchronise. An adjoint enqueue
+ * whose batch exceeds the reservation gathers from the image directly (same
+ * results within FP32 rounding, several times slower). No reference
+ * counterpart. */
+risa_gb_status risa_gb_backprojection_reserve_adjoint(risa_gb_backprojection* h, int max_batch);
+/* Padded pair-sinogram window of the staged variants: per angle, window bin u
+ * holds detector bin u - win_lo, u < win_len (fused_mask 0: every tile; 1: the
+ * tiles the fused circular mask keeps). No reference counterpart (a layout
+ * query, e.g. to count the bytes of the staging pass). */
+risa_gb_status risa_gb_backprojection_window(const risa_gb_backprojection* h, int fused_mask, int* win_lo,
+                                             int* win_len);
 /* Synchronises and returns RISA_GB_ETIMEDOUT if a bounded device-side wait of
  * an earlier enqueue ran out (that tile's pixels were then not written). The
  * asynchronous variants stage detector windows with bulk copies completed on
@@ -360,13 +373,17 @@ risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, fl
 /* Per-stage access for inspection (intermediate device buffers). The engine
  * keeps attenuated fan frames as frame quads -- 4 frames of one plane side by
  * side, [quad][n_fan_proj][n_fan_det][4] float, quads of plane k before those of
- * plane k+1 -- and parallel sinograms per frame, [batch][n_par_proj][n_par_det].
- * The fan buffer holds at least max_batch frames. */
+ * plane k+1 -- and parallel sinograms per frame, [batch][n_par_proj][n_par_det]
+ * (rebinned; with a staged backprojection variant and a radix-16 filter length
+ * the filter writes the backprojection's pair records directly and the
+ * filtered sinogram is not stored). The fan buffer holds at least max_batch
+ * frames. */
 risa_gb_status risa_gb_fbp_intermediates(risa_gb_fbp* h, float** fan, float** par);
 /* Measurement: runs the engine's stages on one batch `reps` times (after a
  * warm-up) with CUDA events on `stream` between them; ms[6] receives the mean
  * durations of defect detection, attenuation (+ repair), rebinning, filter,
- * backprojection staging and the backprojection kernel. Synchronises. */
+ * backprojection staging and the backprojection kernel (staging 0 where the
+ * filter writes the pair records itself). Synchronises. */
 risa_gb_status risa_gb_fbp_time_stages(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane, int batch,
                                        int reps, void* stream, float* ms);
 risa_gb_backprojection* risa_gb_fbp_backprojection(risa_gb_fbp* h);

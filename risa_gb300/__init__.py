@@ -121,7 +121,9 @@ SIGNATURES = {
     "risa_gb_backprojection_variant_count": (_i, []),
     "risa_gb_backprojection_check": (_i, [_vp]),
     "risa_gb_backprojection_reserve": (_i, [_vp, _i]),
+    "risa_gb_backprojection_reserve_adjoint": (_i, [_vp, _i]),
     "risa_gb_backprojection_variant_name": (ctypes.c_char_p, [_i]),
+    "risa_gb_backprojection_window": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "risa_gb_backprojection_time": (_i, [_vp, _vp, _vp, _i, _i, _vp, ctypes.POINTER(ctypes.c_float),
                                          ctypes.POINTER(ctypes.c_float)]),
     "risa_gb_backprojection_destroy": (_i, [_vp]),
@@ -474,6 +476,17 @@ class Backprojection(_Handle):
     def reserve(self, max_batch: int):
         """Device buffer for the staged variants at batches up to max_batch (set-up call)."""
         _check(lib().risa_gb_backprojection_reserve(self._h, max_batch), "backprojection_reserve")
+
+    def reserve_adjoint(self, max_batch: int):
+        """Scratch of the adjoint's fast path at batches up to max_batch (set-up call)."""
+        _check(lib().risa_gb_backprojection_reserve_adjoint(self._h, max_batch), "backprojection_reserve_adjoint")
+
+    def window(self, fused_mask: bool = True):
+        """(win_lo, win_len) of the staged variants' padded pair sinogram."""
+        lo, n = ctypes.c_int(), ctypes.c_int()
+        _check(lib().risa_gb_backprojection_window(self._h, int(fused_mask), ctypes.byref(lo), ctypes.byref(n)),
+               "backprojection_window")
+        return lo.value, n.value
 
     def time(self, sino, img, batch: int, reps: int = 5, stream=None):
         """(staging ms, backprojection kernel ms), CUDA-event means over `reps` launches."""

@@ -207,6 +207,7 @@ struct risa_gb_backprojection {
    int win_lo[2] = {0, 0}, win_len[2] = {0, 0};
    DevBuf pairs, err;
    DevBuf rowbase, colbase;  // adjoint: (hi, lo) line starts [Pp][N]
+   DevBuf adj;               // adjoint: slice-interleaved image copies (reserve_adjoint)
    BPCfg cfg(bool fused_mask) const {
       BPCfg c;
       c.Pp = g.Pp; c.Dp = g.Dp; c.N = g.N;
@@ -227,6 +228,8 @@ struct risa_gb_backprojection {
       c.err = err.as<int>();
       c.rowbase = rowbase.as<float2>();
       c.colbase = colbase.as<float2>();
+      c.adj_scratch = adj.p;
+      c.adj_scratch_bytes = adj.bytes;
       return c;
    }
    // Pair buffer for `batch` slices under every variant. Only set-up calls
@@ -809,14 +812,31 @@ risa_gb_status risa_gb_backprojection_enqueue_adjoint(risa_gb_backprojection* h,
    return RISA_GB_OK;
 }
 
+risa_gb_status risa_gb_backprojection_reserve_adjoint(risa_gb_backprojection* h, int max_batch) {
+   if (!h || max_batch < 1) return fail(RISA_GB_EINVAL, "bad reserve arguments");
+   const size_t need = bp_adjoint_scratch_bytes(max_batch, h->g.N);
+   if (need <= h->adj.bytes) return RISA_GB_OK;
+   RG_CUDA(cudaDeviceSynchronize());
+   return h->adj.alloc(need);
+}
+
+risa_gb_status risa_gb_backprojection_window(const risa_gb_backprojection* h, int fused_mask, int* win_lo,
+                                             int* win_len) {
+   if (!h) return fail(RISA_GB_EINVAL, "null handle");
+   const int m = fused_mask ? 1 : 0;
+   if (win_lo) *win_lo = h->win_lo[m];
+   if (win_len) *win_len = h->win_len[m];
+   return RISA_GB_OK;
+}
+
 risa_gb_status risa_gb_backprojection_check(risa_gb_backprojection* h) {
    if (!h) return fail(RISA_GB_EINVAL, "null handle");
    RG_CUDA(cudaDeviceSynchronize());
    int code = 0;
    RG_CUDA(cudaMemcpy(&code, h->err.p, sizeof(int), cudaMemcpyDeviceToHost));
    if (code)
-      return fail(RISA_GB_ETIMEDOUT, "backprojection: bounded wait ran out or window out of range (code " +
-                                         std::to_string(code) + ")");
+      return fail(RISA_GB_ETIMEDOUT, "bounded wait ran out or window out of range (code " + std::to_string(code) +
+                                         ": 4-5 backprojection, 6 attenuation)");
    return RISA_GB_OK;
 }
 
@@ -944,11 +964,43 @@ risa_gb_status risa_gb_fbp_create(const risa_gb_geometry* gi, const risa_gb_para
                               quad_count(make_quad_map(g.L, 0, max_batch)));
    RG_TRY(h->fan.alloc(sizeof(float) * 4 * (size_t)quads * g.Pf * g.Df));
    RG_TRY(h->par.alloc(sizeof(float) * (size_t)max_batch * g.Pp * g.Dp));
-   if (h->defects) RG_TRY(h->dws.alloc(risa_gb_defects_workspace_bytes(h->defects, max_batch)));
+   if (h->defects)
+      RG_TRY(h->dws.alloc(defects_workspace_bytes(h->defects->cfg.D, max_batch, h->defects->cfg.max_runs, true)));
    RG_TRY(h->mm.alloc(sizeof(unsigned int) * 2 * (size_t)max_batch));
    if (h->p.interp == RISA_GB_INTERP_LINEAR) RG_TRY(h->bp->reserve(max_batch));
    *out = h.release();
    return RISA_GB_OK;
+}
+
+// The engine's attenuation reports its bounded waits in the backprojection's
+// error flag, which every engine run checks.
+static AttenuationCfg engine_atten_cfg(const risa_gb_fbp* h, int plane) {
+   AttenuationCfg c = h->atten->cfg(plane);
+   c.err = h->bp->err.as<int>();
+   return c;
+}
+
+// Filter and backprojection of the engine. With a staged backprojection
+// variant and a radix-16 filter length, the filter writes the pair records
+// itself (one pass instead of filter + staging pass). ev_filtered / ev_staged
+// (optional) are recorded after the filter and after the staging pass.
+static cudaError_t engine_filter_bp(risa_gb_fbp* h, float* par, float* img, int batch, bool fused, cudaStream_t st,
+                                    cudaEvent_t ev_filtered, cudaEvent_t ev_staged) {
+   const FilterCfg fc = h->filt->cfg();
+   const int v = h->bp->variant_for(batch, fused);
+   BPCfg c = h->bp->cfg(fused);
+   const int slices = bp_variant_pair_slices(v);
+   cudaError_t e;
+   if (slices > 0 && filter_pairs_supported(fc)) {
+      e = launch_filter_pairs(par, batch, fc, PairsOut{c.pairs, slices, c.win_lo, c.win_len}, st);
+      c.prefilled = true;
+   } else {
+      e = launch_filter(par, batch, fc, st);
+   }
+   if (e == cudaSuccess && ev_filtered) e = cudaEventRecord(ev_filtered, st);
+   c.mid_event = ev_staged;
+   if (e == cudaSuccess) e = launch_backprojection(par, img, batch, c, v, st);
+   return e;
 }
 
 risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane, int batch,
@@ -961,16 +1013,15 @@ risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* i
    float* par = h->par.as<float>();
    if (h->defects) {
       const DefectCfg& dc = h->defects->cfg;
-      DefectWorkspace ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs);
+      DefectWorkspace ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs, true);
       RG_CUDA(launch_defect_detect(raw, batch, dc, ws, nullptr, st));
-      RG_CUDA(launch_attenuation_quads(raw, fan, batch, h->atten->cfg(plane), &ws, dc.max_runs, st));
+      RG_CUDA(launch_attenuation_quads(raw, fan, batch, engine_atten_cfg(h, plane), &ws, dc.max_runs, st));
    } else {
-      RG_CUDA(launch_attenuation_quads(raw, fan, batch, h->atten->cfg(plane), nullptr, 0, st));
+      RG_CUDA(launch_attenuation_quads(raw, fan, batch, engine_atten_cfg(h, plane), nullptr, 0, st));
    }
    RG_CUDA(launch_fan2para_quads(fan, par, batch, h->f2p->cfg(plane), st));
-   RG_CUDA(launch_filter(par, batch, h->filt->cfg(), st));
    const bool fused = h->p.masking && !h->p.normalize;
-   RG_TRY(bp_run(h->bp, par, img, batch, fused, stream));
+   RG_CUDA(engine_filter_bp(h, par, img, batch, fused, st, nullptr, nullptr));
    if (h->p.normalize)
       RG_CUDA(launch_mask(img, batch, h->g.N, (float)h->p.masking_value, 1, h->mm.as<float>(),
                           h->p.masking, st));
@@ -996,23 +1047,17 @@ risa_gb_status risa_gb_fbp_time_stages(risa_gb_fbp* h, const uint16_t* raw, floa
       DefectWorkspace ws{};
       if (e == cudaSuccess && h->defects) {
          const DefectCfg& dc = h->defects->cfg;
-         ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs);
+         ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs, true);
          e = launch_defect_detect(raw, batch, dc, ws, nullptr, st);
       }
       if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
       if (e == cudaSuccess)
-         e = launch_attenuation_quads(raw, fan, batch, h->atten->cfg(plane), h->defects ? &ws : nullptr,
+         e = launch_attenuation_quads(raw, fan, batch, engine_atten_cfg(h, plane), h->defects ? &ws : nullptr,
                                       h->defects ? h->defects->cfg.max_runs : 0, st);
       if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
       if (e == cudaSuccess) e = launch_fan2para_quads(fan, par, batch, h->f2p->cfg(plane), st);
       if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
-      if (e == cudaSuccess) e = launch_filter(par, batch, h->filt->cfg(), st);
-      if (e == cudaSuccess) e = cudaEventRecord(ev[4], st);
-      if (e == cudaSuccess) {
-         BPCfg c = h->bp->cfg(fused);
-         c.mid_event = ev[5];
-         e = launch_backprojection(par, img, batch, c, h->bp->variant_for(batch, fused), st);
-      }
+      if (e == cudaSuccess) e = engine_filter_bp(h, par, img, batch, fused, st, ev[4], ev[5]);
       if (e == cudaSuccess) e = cudaEventRecord(ev[6], st);
       if (e == cudaSuccess) e = cudaEventSynchronize(ev[6]);
       for (int k = 0; k < 6 && e == cudaSuccess; ++k) {

@@ -9,6 +9,7 @@
 // mask is a bit mask. The defect repair of the DetectorInterpolation stage
 // can be fused: rows are staged in shared memory, repaired run by run, then
 // converted.
+#include "async_copy.h"
 #include "kernels.h"
 #include "risa_gb300.h"
 
@@ -318,6 +319,116 @@ __global__ void __launch_bounds__(kThreads) attenuation_quads(const uint16_t* __
       }
    }
 }
+// A uint16 count as float: 2^23 + raw has the count in its low mantissa bits,
+// so one bit-or and one exact subtraction give the same value as (float)raw
+// without the conversion unit.
+__device__ __forceinline__ float u16_to_float(unsigned raw) {
+   return __fsub_rn(__uint_as_float(0x4B000000u | raw), 8388608.0f);
+}
+__device__ __forceinline__ float atten_count(unsigned raw, float dark, float logden) {
+   const float num = fmaxf(__fsub_rn(u16_to_float(raw), dark), kClamp);
+   return __fsub_rn(logden, __logf(num));
+}
+
+// Quad attenuation for detector-major frames with D % 8 == 0 and 16-byte
+// aligned rows. The kQRows raw rows of each of the quad's 4 frames are one
+// contiguous range of a frame: thread 0 copies the four ranges into shared
+// memory with bulk copies completing on one mbarrier (no thread issues a load
+// per sample). NONE-mode defects are then repaired from the per-frame fix
+// lists -- one independent update per defective column and row, all lanes
+// busy -- and each thread converts a pair of adjacent columns of the 4 frames
+// (one 32-bit shared load per frame, two 16-byte streaming stores).
+// The bounded wait records code 6 in cfg.err and returns.
+__global__ void __launch_bounds__(kThreads) attenuation_quads_bulk(const uint16_t* __restrict__ raw,
+                                                                   float4* __restrict__ fanq, AttenuationCfg cfg,
+                                                                   QuadMap qm, const int* __restrict__ fix_counts,
+                                                                   const DefectFix* __restrict__ fixes) {
+   extern __shared__ __align__(16) uint16_t tile[];  // [4][kQRows][D]
+   __shared__ __align__(8) uint64_t bar;
+   __shared__ int s_fail;
+   const int D = cfg.D, P = cfg.P;
+   const size_t fs = (size_t)P * D;
+   const int q = blockIdx.y;
+   const int k = quad_plane(qm, q);
+   const int y0 = blockIdx.x * kQRows;
+   const int rows = min(kQRows, P - y0);
+   int fr[4];
+#pragma unroll
+   for (int j = 0; j < 4; ++j) fr[j] = quad_frame(qm, q, j);
+   if (threadIdx.x == 0) {
+      async::mbar_init(&bar, 1);
+      async::mbar_init_fence();
+      s_fail = 0;
+   }
+   __syncthreads();
+   if (threadIdx.x == 0) {
+      const uint32_t bytes = (uint32_t)(sizeof(uint16_t) * rows * D);
+      uint32_t total = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) total += fr[j] >= 0 ? bytes : 0u;
+      async::mbar_arrive_expect_tx(&bar, total);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+         if (fr[j] >= 0)
+            async::bulk_load(tile + (size_t)j * kQRows * D, raw + (size_t)fr[j] * fs + (size_t)y0 * D, bytes, &bar);
+   }
+   if (!async::mbar_wait(&bar, 0, cfg.err, 6)) s_fail = 1;
+   __syncthreads();
+   if (s_fail) {  // leave no copy in flight into this CTA's shared memory
+      if (threadIdx.x == 0) async::mbar_wait_quiet(&bar, 0);
+      return;
+   }
+   if (fixes) {
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int jr = warp; jr < 4 * kQRows; jr += kThreads / 32) {
+         const int j = jr / kQRows, r = jr % kQRows;
+         const int fj = quad_frame(qm, q, j);
+         if (r >= rows || fj < 0) continue;
+         const int n = __ldg(fix_counts + fj);
+         const DefectFix* fl = fixes + (size_t)fj * D;
+         uint16_t* row = tile + (size_t)jr * D;
+         for (int i = lane; i < n; i += 32) {
+            const DefectFix e = fl[i];
+            row[e.col] = defect_mix(row[e.left], row[e.right], e.w0, e.w1, cfg.quirk);
+         }
+      }
+      __syncthreads();
+   }
+   const int H = D >> 1;  // column pairs per row
+   const int total = rows * H;
+   const float2* dk2 = reinterpret_cast<const float2*>(cfg.dark + (size_t)k * D);
+   const float2* ld2 = reinterpret_cast<const float2*>(cfg.logden + (size_t)k * fs + (size_t)y0 * D);
+   const uint32_t* t32 = reinterpret_cast<const uint32_t*>(tile);
+   const int fstride = kQRows * H;  // 32-bit words between the frames of the tile
+   float4* dst0 = fanq + ((size_t)q * P + y0) * D;
+   int r = threadIdx.x / H, xp = threadIdx.x - r * H;
+   for (int i = threadIdx.x; i < total; i += kThreads) {
+      const float2 d = __ldg(dk2 + xp), l = __ldg(ld2 + i);
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) w[j] = t32[j * fstride + i];
+      float a[4], b[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+         a[j] = fr[j] >= 0 ? atten_count(w[j] & 0xFFFFu, d.x, l.x) : 0.f;
+         b[j] = fr[j] >= 0 ? atten_count(w[j] >> 16, d.y, l.y) : 0.f;
+      }
+      if (cfg.mask) {
+         const int x = 2 * xp;
+         const uint32_t bits = __ldg(cfg.mask + (size_t)(y0 + r) * cfg.wpr + (x >> 5)) >> (x & 31);
+         if (!(bits & 1u)) a[0] = a[1] = a[2] = a[3] = 0.f;
+         if (!(bits & 2u)) b[0] = b[1] = b[2] = b[3] = 0.f;
+      }
+      float4* dst = dst0 + 2 * (size_t)i;
+      __stcs(dst, make_float4(a[0], a[1], a[2], a[3]));
+      __stcs(dst + 1, make_float4(b[0], b[1], b[2], b[3]));
+      xp += kThreads;
+      while (xp >= H) {
+         xp -= H;
+         ++r;
+      }
+   }
+}
 }  // namespace
 
 cudaError_t launch_attenuation(const uint16_t* raw, float* out, int batch,
@@ -350,11 +461,25 @@ cudaError_t launch_attenuation_quads(const uint16_t* raw, float* fanq, int batch
    if (batch <= 0) return cudaSuccess;
    const QuadMap qm = make_quad_map(cfg.L, cfg.plane, batch);
    const size_t smem = sizeof(uint16_t) * 4 * kQRows * (size_t)cfg.D;
+   dim3 grid((cfg.P + kQRows - 1) / kQRows, quad_count(qm));
+   // bulk-copy path: whole rows per frame, NONE-mode repair from fix lists
+   const bool bulk = cfg.err && cfg.modules <= 0 && cfg.D % 8 == 0 && ((uintptr_t)raw & 15u) == 0 &&
+                     (!runs || (cfg.quirk != RISA_GB_QUIRKS_RISA && runs->fixes));
+   if (bulk) {
+      if (smem > 48 * 1024) {
+         cudaError_t e = cudaFuncSetAttribute(attenuation_quads_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem);
+         if (e != cudaSuccess) return e;
+      }
+      attenuation_quads_bulk<<<grid, kThreads, smem, st>>>(raw, reinterpret_cast<float4*>(fanq), cfg, qm,
+                                                           runs ? runs->fix_counts : nullptr,
+                                                           runs ? runs->fixes : nullptr);
+      return cudaGetLastError();
+   }
    if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(attenuation_quads, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
    }
-   dim3 grid((cfg.P + kQRows - 1) / kQRows, quad_count(qm));
    attenuation_quads<<<grid, kThreads, smem, st>>>(raw, reinterpret_cast<float4*>(fanq), cfg, qm,
                                                    runs ? runs->counts : nullptr, runs ? runs->runs : nullptr,
                                                    max_runs);

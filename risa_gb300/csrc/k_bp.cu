@@ -642,10 +642,13 @@ cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& 
    if (!cfg.pairs || !cfg.err || cfg.win_len < wlen) return cudaErrorInvalidValue;
    const int groups = (batch + S - 1) / S;
    if ((size_t)groups * S * cfg.Pp * cfg.win_len * sizeof(float2) > cfg.pairs_bytes) return cudaErrorInvalidValue;
-   bp_pairs_fill<S><<<dim3((cfg.win_len + 255) / 256, cfg.Pp, groups), 256, 0, st>>>(
-       sino, reinterpret_cast<float4*>(cfg.pairs), batch, cfg.Pp, cfg.Dp, cfg.win_lo, cfg.win_len);
-   cudaError_t e = cudaGetLastError();
-   if (e != cudaSuccess) return e;
+   cudaError_t e = cudaSuccess;
+   if (!cfg.prefilled) {
+      bp_pairs_fill<S><<<dim3((cfg.win_len + 255) / 256, cfg.Pp, groups), 256, 0, st>>>(
+          sino, reinterpret_cast<float4*>(cfg.pairs), batch, cfg.Pp, cfg.Dp, cfg.win_lo, cfg.win_len);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+   }
    if (cfg.mid_event && (e = cudaEventRecord(cfg.mid_event, st)) != cudaSuccess) return e;
    auto kern = bp_linear_async<S, ACH, PACKED, PPT>;
    if (smem > 48 * 1024) {
@@ -759,11 +762,120 @@ __global__ void __launch_bounds__(128) bp_adjoint(const float* __restrict__ img,
    for (int s = 0; s < SB; ++s)
       if (s0 + s < batch) sino[((size_t)(s0 + s) * cfg.Pp + i) * cfg.Dp + k] = acc[s] * cfg.norm;
 }
+// Slice-interleaved copies of the image for the adjoint: P[g][y][x][8] and
+// its transpose PT[g][x][y][8] hold slices 8g..8g+7 (zero past the batch), so
+// a ray walking rows of P (angles with |a| >= |b|) or rows of PT (the others)
+// reads the 8 slices of a pixel with two 16-byte loads from consecutive
+// addresses across the warp. One CTA transposes a 32 x 32 pixel tile of all 8
+// slices of a group through shared memory.
+__global__ void __launch_bounds__(256) bp_adjoint_layout(const float* __restrict__ img, float4* __restrict__ P,
+                                                         float4* __restrict__ PT, int N, int batch) {
+   __shared__ float tile[8][32][33];
+   const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32, g = blockIdx.z;
+   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+   const size_t plane = (size_t)N * N;
+#pragma unroll
+   for (int s = 0; s < 8; ++s) {
+      const int b = 8 * g + s;
+      for (int yy = ty; yy < 32; yy += 8) {
+         const int y = y0 + yy, x = x0 + tx;
+         tile[s][yy][tx] = (b < batch && y < N && x < N) ? __ldg(img + (size_t)b * plane + (size_t)y * N + x) : 0.f;
+      }
+   }
+   __syncthreads();
+   float4* Pg = P + (size_t)g * plane * 2;
+   float4* PTg = PT + (size_t)g * plane * 2;
+   for (int yy = ty; yy < 32; yy += 8) {
+      const int y = y0 + yy, x = x0 + tx;
+      if (y < N && x < N) {  // pixel (y, x): row y of P
+         const size_t o = ((size_t)y * N + x) * 2;
+         Pg[o] = make_float4(tile[0][yy][tx], tile[1][yy][tx], tile[2][yy][tx], tile[3][yy][tx]);
+         Pg[o + 1] = make_float4(tile[4][yy][tx], tile[5][yy][tx], tile[6][yy][tx], tile[7][yy][tx]);
+      }
+      const int xt = x0 + yy, yt = y0 + tx;  // pixel (yt, xt): row xt of PT
+      if (xt < N && yt < N) {
+         const size_t o = ((size_t)xt * N + yt) * 2;
+         PTg[o] = make_float4(tile[0][tx][yy], tile[1][tx][yy], tile[2][tx][yy], tile[3][tx][yy]);
+         PTg[o + 1] = make_float4(tile[4][tx][yy], tile[5][tx][yy], tile[6][tx][yy], tile[7][tx][yy]);
+      }
+   }
+}
+
+// The adjoint over the interleaved layout: as bp_adjoint with 8 slices per
+// thread, the ray always walking rows (of P, or of PT for steep angles), and
+// the visited pixel range [floor(ja), ceil(jb)]: the range ends carry an
+// error of ~1e-6 * N / |step| pixels (< 1e-3), far below one pixel, and every
+// visited pixel is still tested exactly (|t' - k| < 1).
+__global__ void __launch_bounds__(128) bp_adjoint_rows(const float4* __restrict__ P, const float4* __restrict__ PT,
+                                                       float* __restrict__ sino, BPCfg cfg, int batch) {
+   extern __shared__ float2 s_line[];  // this angle's line starts [N]
+   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+   const int i = blockIdx.y;
+   const int g = blockIdx.z;
+   const int N = cfg.N;
+   const float a = __ldg(cfg.a + i), b = __ldg(cfg.b + i);
+   const bool along_x = fabsf(a) >= fabsf(b);
+   const float2* line = (along_x ? cfg.rowbase : cfg.colbase) + (size_t)i * N;
+   for (int r = threadIdx.x; r < N; r += blockDim.x) s_line[r] = __ldg(line + r);
+   __syncthreads();
+   if (k >= cfg.Dp) return;
+   const float s_hi = along_x ? a : b;
+   const float s_lo = (float)((along_x ? __ldg(cfg.ad + i) : __ldg(cfg.bd + i)) - (double)s_hi);
+   const float inv = 1.0f / s_hi;  // |s_hi| >= scale / sqrt(2) > 0
+   const float4* im = (along_x ? P : PT) + (size_t)g * N * N * 2;
+   const float kf = (float)k;
+   float acc[8];
+#pragma unroll
+   for (int s = 0; s < 8; ++s) acc[s] = 0.f;
+   for (int r = 0; r < N; ++r) {
+      const float2 hb = s_line[r];
+      const float t_hi = hb.x - kf, t_lo = hb.y;
+      const float t0 = t_hi + t_lo;
+      float ja = (-1.f - t0) * inv, jb = (1.f - t0) * inv;
+      if (ja > jb) {
+         const float tt = ja;
+         ja = jb;
+         jb = tt;
+      }
+      if (jb < 0.f || ja > (float)(N - 1)) continue;
+      const int js = max(0, (int)floorf(ja)), je = min(N - 1, (int)ceilf(jb));
+      const float4* row = im + (size_t)r * N * 2;
+      for (int j = js; j <= je; ++j) {
+         const float jf = (float)j;
+         const float d = fabsf(fmaf(jf, s_hi, t_hi) + fmaf(jf, s_lo, t_lo));
+         if (d < 1.f) {
+            const float w = 1.f - d;
+            const float4 v0 = __ldg(row + 2 * j), v1 = __ldg(row + 2 * j + 1);
+            acc[0] = fmaf(w, v0.x, acc[0]);
+            acc[1] = fmaf(w, v0.y, acc[1]);
+            acc[2] = fmaf(w, v0.z, acc[2]);
+            acc[3] = fmaf(w, v0.w, acc[3]);
+            acc[4] = fmaf(w, v1.x, acc[4]);
+            acc[5] = fmaf(w, v1.y, acc[5]);
+            acc[6] = fmaf(w, v1.z, acc[6]);
+            acc[7] = fmaf(w, v1.w, acc[7]);
+         }
+      }
+   }
+#pragma unroll
+   for (int s = 0; s < 8; ++s)
+      if (8 * g + s < batch) sino[((size_t)(8 * g + s) * cfg.Pp + i) * cfg.Dp + k] = acc[s] * cfg.norm;
+}
 }  // namespace
+
+size_t bp_adjoint_scratch_bytes(int batch, int N) {
+   return batch <= 0 ? 0 : sizeof(float) * 2 * 8 * (size_t)((batch + 7) / 8) * N * N;
+}
 
 int bp_variant_count() { return kNumVariants; }
 const char* bp_variant_name(int v) {
    return (v >= 0 && v < kNumVariants) ? kVariants[v].name : "invalid";
+}
+
+int bp_variant_pair_slices(int variant) {
+   if (variant < 0 || variant >= kNumVariants) return 0;
+   const BPVariant& v = kVariants[variant];
+   return (v.kind == kAsync || v.kind == kAsyncPacked) ? v.slices : 0;
 }
 
 size_t bp_pairs_bytes(int variant, int batch, int Pp, int win_len) {
@@ -860,6 +972,16 @@ cudaError_t launch_backprojection_adjoint(const float* img, float* sino, int bat
    // slices share the geometry: each thread applies its weights to SB slices
    const size_t smem = sizeof(float2) * (size_t)cfg.N;
    if (smem > 48 * 1024) return cudaErrorInvalidConfiguration;  // N <= 6144
+   if (cfg.adj_scratch && cfg.adj_scratch_bytes >= bp_adjoint_scratch_bytes(batch, cfg.N)) {
+      const int groups = (batch + 7) / 8;
+      float4* P = reinterpret_cast<float4*>(cfg.adj_scratch);
+      float4* PT = P + (size_t)groups * cfg.N * cfg.N * 2;
+      dim3 lg((cfg.N + 31) / 32, (cfg.N + 31) / 32, groups);
+      bp_adjoint_layout<<<lg, 256, 0, st>>>(img, P, PT, cfg.N, batch);
+      dim3 grid((cfg.Dp + 127) / 128, cfg.Pp, groups);
+      bp_adjoint_rows<<<grid, 128, smem, st>>>(P, PT, sino, cfg, batch);
+      return cudaGetLastError();
+   }
    if (batch >= 8) {
       dim3 grid((cfg.Dp + 127) / 128, cfg.Pp, (batch + 7) / 8);
       bp_adjoint<8><<<grid, 128, smem, st>>>(img, sino, cfg, batch);

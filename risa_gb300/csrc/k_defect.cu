@@ -13,6 +13,8 @@
 //   3. defect_repair (or the attenuation kernel, fused): each row applies the
 //      runs in list order, so in-place dependencies between runs resolve as
 //      in the reference's sequential loop.
+#include <algorithm>
+
 #include "kernels.h"
 #include "risa_gb300.h"
 
@@ -61,10 +63,61 @@ __global__ void __launch_bounds__(kStatThreads) defect_stats(const uint16_t* __r
    atomicMin(&s->mn, mn);
 }
 
+// Detector-major frames with D % 8 == 0 and 16-byte aligned rows: each thread
+// takes 8 adjacent columns (one 16-byte load per row), keeps their max/min as
+// packed 16-bit pairs and their total variation in 32 bits (at most
+// kStatRowsVec * 65535 per chunk), and adds the chunk's results atomically.
+// Rows are loaded kStatBatch at a time so that many loads are in flight.
+constexpr int kStatRowsVec = 32;
+constexpr int kStatBatch = 8;
+__global__ void __launch_bounds__(256) defect_stats_vec8(const uint16_t* __restrict__ frames,
+                                                         ColStats* __restrict__ st, int P, int D) {
+   const int o = blockIdx.x * blockDim.x + threadIdx.x;  // column octet
+   if (8 * o >= D) return;
+   const int r0 = blockIdx.y * kStatRowsVec;
+   const int r1 = min(r0 + kStatRowsVec, P - 1);  // pairs (p, p+1) with p < r1
+   if (r0 >= r1) return;
+   const uint4* f = reinterpret_cast<const uint4*>(frames + (size_t)blockIdx.z * P * D) + o;
+   const size_t rs = (size_t)D / 8;
+   uint4 prev = __ldg(f + (size_t)r0 * rs);
+   uint32_t mx[4] = {prev.x, prev.y, prev.z, prev.w}, mn[4] = {prev.x, prev.y, prev.z, prev.w};
+   uint32_t tv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+   for (int p = r0; p < r1; p += kStatBatch) {
+      uint4 nx[kStatBatch];
+#pragma unroll
+      for (int i = 0; i < kStatBatch; ++i)
+         nx[i] = (p + i < r1) ? __ldg(f + (size_t)(p + 1 + i) * rs) : prev;
+#pragma unroll
+      for (int i = 0; i < kStatBatch; ++i) {
+         if (p + i >= r1) break;
+         const uint32_t a[4] = {prev.x, prev.y, prev.z, prev.w}, b[4] = {nx[i].x, nx[i].y, nx[i].z, nx[i].w};
+#pragma unroll
+         for (int j = 0; j < 4; ++j) {
+            tv[2 * j] = __sad(a[j] & 0xFFFFu, b[j] & 0xFFFFu, tv[2 * j]);
+            tv[2 * j + 1] = __sad(a[j] >> 16, b[j] >> 16, tv[2 * j + 1]);
+            mx[j] = __vmaxu2(mx[j], a[j]);
+            mn[j] = __vminu2(mn[j], a[j]);
+         }
+         prev = nx[i];
+      }
+   }
+   ColStats* s = st + (size_t)blockIdx.z * D + 8 * o;
+#pragma unroll
+   for (int j = 0; j < 4; ++j) {
+      atomicAdd(&s[2 * j].tv, (unsigned long long)tv[2 * j]);
+      atomicAdd(&s[2 * j + 1].tv, (unsigned long long)tv[2 * j + 1]);
+      atomicMax(&s[2 * j].mx, mx[j] & 0xFFFFu);
+      atomicMax(&s[2 * j + 1].mx, mx[j] >> 16);
+      atomicMin(&s[2 * j].mn, mn[j] & 0xFFFFu);
+      atomicMin(&s[2 * j + 1].mn, mn[j] >> 16);
+   }
+}
+
 // One CTA per frame. Dynamic shared memory: var[D] (double) then flags[D+1].
 __global__ void defect_flags(const ColStats* __restrict__ st, DefectCfg cfg,
                              int32_t* __restrict__ flags_out, int* __restrict__ counts,
-                             DefectRun* __restrict__ runs) {
+                             DefectRun* __restrict__ runs, int* __restrict__ fix_counts,
+                             DefectFix* __restrict__ fixes) {
    extern __shared__ double smem_d[];
    const int D = cfg.D;
    double* var = smem_d;
@@ -118,10 +171,11 @@ __global__ void defect_flags(const ColStats* __restrict__ st, DefectCfg cfg,
       // starts at a flagged column after a good one) and their order in the
       // list does not change the repaired frame. At most D/2 runs exist, below
       // max_runs.
-      __shared__ int s_runs, s_good;
+      __shared__ int s_runs, s_good, s_fixes;
       if (threadIdx.x == 0) {
          s_runs = 0;
          s_good = 0;
+         s_fixes = 0;
       }
       __syncthreads();
       for (int d = threadIdx.x; d < D; d += blockDim.x)
@@ -140,11 +194,27 @@ __global__ void defect_flags(const ColStats* __restrict__ st, DefectCfg cfg,
                r.left = (uint16_t)(d == 0 ? uD - 1u : d - 1u);
                r.right = (uint16_t)((d + len) % uD);
                out[slot] = r;
+               if (fixes) {  // the run's columns, each with its own weights
+                  DefectFix* fx = fixes + (size_t)f * D + atomicAdd(&s_fixes, (int)len);
+                  for (unsigned m = 0; m < len; ++m) {
+                     DefectFix e;
+                     e.col = (uint16_t)((d + m) % uD);
+                     e.left = r.left;
+                     e.right = r.right;
+                     e.pad = 0;
+                     e.w1 = defect_w1((int)m, (int)len);
+                     e.w0 = __fsub_rn(1.0f, e.w1);
+                     fx[m] = e;
+                  }
+               }
             }
          }
       }
       __syncthreads();
-      if (threadIdx.x == 0) counts[f] = s_runs < cfg.max_runs ? s_runs : cfg.max_runs;
+      if (threadIdx.x == 0) {
+         counts[f] = s_runs < cfg.max_runs ? s_runs : cfg.max_runs;
+         if (fix_counts) fix_counts[f] = s_fixes;
+      }
       return;
    }
    if (threadIdx.x != 0) return;
@@ -192,13 +262,15 @@ __global__ void defect_repair(uint16_t* __restrict__ frames, DefectCfg cfg,
 }
 }  // namespace
 
-size_t defects_workspace_bytes(int D, int batch, int max_runs) {
+size_t defects_workspace_bytes(int D, int batch, int max_runs, bool fixes) {
    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
-   return align(sizeof(ColStats) * (size_t)D * batch) + align(sizeof(int) * (size_t)batch) +
-          align(sizeof(DefectRun) * (size_t)max_runs * batch);
+   size_t n = align(sizeof(ColStats) * (size_t)D * batch) + align(sizeof(int) * (size_t)batch) +
+              align(sizeof(DefectRun) * (size_t)max_runs * batch);
+   if (fixes) n += align(sizeof(int) * (size_t)batch) + align(sizeof(DefectFix) * (size_t)D * batch);
+   return n;
 }
 
-DefectWorkspace defects_carve(void* ws, int D, int batch, int max_runs) {
+DefectWorkspace defects_carve(void* ws, int D, int batch, int max_runs, bool fixes) {
    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
    char* p = static_cast<char*>(ws);
    DefectWorkspace w;
@@ -207,7 +279,14 @@ DefectWorkspace defects_carve(void* ws, int D, int batch, int max_runs) {
    w.counts = reinterpret_cast<int*>(p);
    p += align(sizeof(int) * (size_t)batch);
    w.runs = reinterpret_cast<DefectRun*>(p);
-   (void)max_runs;
+   p += align(sizeof(DefectRun) * (size_t)max_runs * batch);
+   w.fix_counts = nullptr;
+   w.fixes = nullptr;
+   if (fixes) {
+      w.fix_counts = reinterpret_cast<int*>(p);
+      p += align(sizeof(int) * (size_t)batch);
+      w.fixes = reinterpret_cast<DefectFix*>(p);
+   }
    return w;
 }
 
@@ -232,11 +311,20 @@ cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const Defect
    if (batch <= 0) return cudaSuccess;
    const int n = cfg.D * batch;
    defect_stats_init<<<(n + 255) / 256, 256, 0, st>>>(ws.stats, n);
-   dim3 grid((cfg.D + kStatThreads - 1) / kStatThreads, (cfg.P - 1 + kStatRows - 1) / kStatRows,
-             batch);
-   defect_stats<<<grid, kStatThreads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D, cfg.modules);
+   if (cfg.modules <= 0 && cfg.D % 8 == 0 && ((uintptr_t)frames & 15u) == 0) {
+      // one block spans a frame's column octets where it can (D <= 2048)
+      const int octets = cfg.D / 8;
+      const int threads = std::min(256, (octets + 31) / 32 * 32);
+      dim3 grid((octets + threads - 1) / threads, (cfg.P - 1 + kStatRowsVec - 1) / kStatRowsVec, batch);
+      defect_stats_vec8<<<grid, threads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D);
+   } else {
+      dim3 grid((cfg.D + kStatThreads - 1) / kStatThreads, (cfg.P - 1 + kStatRows - 1) / kStatRows,
+                batch);
+      defect_stats<<<grid, kStatThreads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D, cfg.modules);
+   }
    const size_t smem = sizeof(double) * cfg.D + sizeof(int) * (cfg.D + 1);
-   defect_flags<<<batch, 256, smem, st>>>(ws.stats, cfg, flags_out, ws.counts, ws.runs);
+   defect_flags<<<batch, 256, smem, st>>>(ws.stats, cfg, flags_out, ws.counts, ws.runs, ws.fix_counts,
+                                          ws.fixes);
    return cudaGetLastError();
 }
 

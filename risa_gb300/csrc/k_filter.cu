@@ -230,6 +230,71 @@ cudaError_t launch_r16(float* sino, int total_rows, const FilterCfg& cfg, cudaSt
    return cudaGetLastError();
 }
 
+// Filter and backprojection staging in one pass. A group's row pair is one
+// angle of two consecutive slices (2h, 2h+1) of the batch, so after the
+// inverse transform both filtered rows of that angle are in the group's
+// shared buffer and the group writes the padded pair records the staged
+// backprojection reads,
+//    pairs[g][angle][h][u] = (mid_2h, mid_2h+1, diff_2h, diff_2h+1),  k = u - win_lo,
+//    mid = (q[k] + q[k+1]) / 2, diff = q[k+1] - q[k], q = 0 outside the detector,
+// for every window bin u -- the filtered sinogram itself is never written.
+template <int LEN>
+__global__ void __launch_bounds__(256, 2) filter_rows_r16_pairs(const float* __restrict__ sino, int batch,
+                                                                FilterCfg cfg, PairsOut po) {
+   constexpr int TPF = LEN / 16, FPB = 256 / TPF, PL = LEN + LEN / 16;
+   using P = R16Plan<LEN>;
+   extern __shared__ float2 sm[];
+   const int local = threadIdx.x / TPF, lt = threadIdx.x % TPF;
+   const int Pp = cfg.rows, Dp = cfg.Dp;
+   const int pair = blockIdx.x * FPB + local;  // (slice pair, angle)
+   const int sp = pair / Pp, ang = pair - sp * Pp;
+   const int s0 = 2 * sp;
+   const bool has_a = s0 < batch, has_b = s0 + 1 < batch;
+   const float* row_a = sino + ((size_t)(has_a ? s0 : 0) * Pp + ang) * Dp;
+   const float* row_b = sino + ((size_t)(has_b ? s0 + 1 : 0) * Pp + ang) * Dp;
+   float2* buf = sm + local * PL;
+   float2 v[16];
+#pragma unroll
+   for (int r = 0; r < 16; ++r) {
+      const int n = lt + r * TPF;
+      v[r] = make_float2((has_a && n < Dp) ? row_a[n] : 0.f, (has_b && n < Dp) ? row_b[n] : 0.f);
+   }
+   r16_filter_core<LEN>(v, buf, lt, cfg.twp, cfg.h, cfg.adjoint != 0);
+   __syncthreads();
+#pragma unroll
+   for (int b = 0; b < 16 / P::R3; ++b)
+#pragma unroll
+      for (int r = 0; r < P::R3; ++r) {
+         const int n = r16_time_index<LEN>(lt, b, r);
+         if (n < Dp) buf[pad16(n)] = make_float2(v[b * P::R3 + r].x, has_b ? -v[b * P::R3 + r].y : 0.f);
+      }
+   __syncthreads();
+   if (!has_a) return;
+   const int g = s0 / po.S, h = (s0 % po.S) >> 1;
+   float4* out = reinterpret_cast<float4*>(po.pairs) + (((size_t)g * Pp + ang) * (po.S / 2) + h) * po.wp;
+   for (int u = lt; u < po.wp; u += TPF) {
+      const int k = u - po.win_lo;
+      const float2 q0 = (k >= 0 && k < Dp) ? buf[pad16(k)] : make_float2(0.f, 0.f);
+      const float2 q1 = (k + 1 >= 0 && k + 1 < Dp) ? buf[pad16(k + 1)] : make_float2(0.f, 0.f);
+      out[u] = make_float4(0.5f * (q0.x + q1.x), 0.5f * (q0.y + q1.y), q1.x - q0.x, q1.y - q0.y);
+   }
+}
+
+template <int LEN>
+cudaError_t launch_r16_pairs(const float* sino, int batch, const FilterCfg& cfg, const PairsOut& po,
+                             cudaStream_t st) {
+   constexpr int TPF = LEN / 16, FPB = 256 / TPF;
+   const size_t smem = sizeof(float2) * (size_t)FPB * (LEN + LEN / 16);
+   if (smem > 48 * 1024) {
+      cudaError_t e =
+          cudaFuncSetAttribute(filter_rows_r16_pairs<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+   }
+   const int pairs = (batch + 1) / 2 * cfg.rows;
+   filter_rows_r16_pairs<LEN><<<(pairs + FPB - 1) / FPB, 256, smem, st>>>(sino, batch, cfg, po);
+   return cudaGetLastError();
+}
+
 // One CTA: invert the summed (conjugated) spectrum, scale by 1/len, map lags to taps.
 __global__ void __launch_bounds__(kThreads) filter_grad_finish(const float2* __restrict__ spec, FilterCfg cfg,
                                                                int n_taps, int center, float* __restrict__ grad) {
@@ -304,6 +369,23 @@ std::vector<float2> filter_pass_twiddles(int len) {
    add(r2, 16);
    add(r3, ns3);
    return t;
+}
+
+bool filter_pairs_supported(const FilterCfg& cfg) {
+   return cfg.twp && (cfg.len == 512 || cfg.len == 1024 || cfg.len == 2048 || cfg.len == 4096);
+}
+
+cudaError_t launch_filter_pairs(const float* sino, int batch, const FilterCfg& cfg, const PairsOut& po,
+                                cudaStream_t st) {
+   if (batch <= 0) return cudaSuccess;
+   if (!po.pairs || po.S < 2 || po.S % 2 || po.wp <= 0) return cudaErrorInvalidValue;
+   switch (filter_pairs_supported(cfg) ? cfg.len : 0) {
+      case 512: return launch_r16_pairs<512>(sino, batch, cfg, po, st);
+      case 1024: return launch_r16_pairs<1024>(sino, batch, cfg, po, st);
+      case 2048: return launch_r16_pairs<2048>(sino, batch, cfg, po, st);
+      case 4096: return launch_r16_pairs<4096>(sino, batch, cfg, po, st);
+      default: return cudaErrorNotSupported;
+   }
 }
 
 cudaError_t launch_filter(float* sino, int batch, const FilterCfg& cfg, cudaStream_t st) {

@@ -24,6 +24,14 @@ struct ColStats {
 struct DefectRun {
    uint16_t start, len, left, right;
 };
+// One defective column of a frame in NONE mode, where every run is repaired
+// from good columns only: its repaired value is w0*left + w1*right with the
+// weights of its place in its run, precomputed once per frame, so the repair
+// of each row is one independent update per defective column.
+struct __align__(16) DefectFix {
+   uint16_t col, left, right, pad;
+   float w1, w0;
+};
 struct DefectCfg {
    int P, D;
    double thresh_min, thresh_max;
@@ -52,27 +60,35 @@ cudaError_t launch_reorder(const uint16_t* in, uint16_t* out, int modules, int P
 // of a float rounding midpoint unless it equals one, so the single IEEE float
 // division gives the same bits without FP64 arithmetic. RISA mode truncates
 // to uint16 as the reference's conversion does; NONE mode rounds to nearest.
-__device__ __forceinline__ uint16_t defect_value(unsigned left, unsigned right, int m, int len,
-                                                 int quirk) {
-   const float w1 = __fdiv_rn((float)(m + 1), (float)(len + 1));
-   const float w0 = __fsub_rn(1.0f, w1);
+__device__ __forceinline__ float defect_w1(int m, int len) {
+   return __fdiv_rn((float)(m + 1), (float)(len + 1));
+}
+__device__ __forceinline__ uint16_t defect_mix(unsigned left, unsigned right, float w0, float w1, int quirk) {
    const float v = __fadd_rn(__fmul_rn(w0, (float)left), __fmul_rn(w1, (float)right));
    if (quirk == 1) return (uint16_t)__float2uint_rz(v);
    return (uint16_t)__float2uint_rz(floorf(__fadd_rn(v, 0.5f)));
+}
+__device__ __forceinline__ uint16_t defect_value(unsigned left, unsigned right, int m, int len,
+                                                 int quirk) {
+   const float w1 = defect_w1(m, len);
+   return defect_mix(left, right, __fsub_rn(1.0f, w1), w1, quirk);
 }
 template <class Row>
 __device__ __forceinline__ uint16_t repair_value(const Row& row, const DefectRun& run, int m, int quirk) {
    return defect_value(row[run.left], row[run.right], m, run.len, quirk);
 }
 #endif
-size_t defects_workspace_bytes(int D, int batch, int max_runs);
-// Workspace layout: [batch*D ColStats][batch int run counts][batch*max_runs DefectRun]
+// Workspace layout: [batch*D ColStats][batch int run counts][batch*max_runs DefectRun],
+// with `fixes`: then [batch int fix counts][batch*D DefectFix] (NONE mode only).
+size_t defects_workspace_bytes(int D, int batch, int max_runs, bool fixes = false);
 struct DefectWorkspace {
    ColStats* stats;
    int* counts;
    DefectRun* runs;
+   int* fix_counts;   // nullptr without fix lists
+   DefectFix* fixes;  // [batch][D]
 };
-DefectWorkspace defects_carve(void* ws, int D, int batch, int max_runs);
+DefectWorkspace defects_carve(void* ws, int D, int batch, int max_runs, bool fixes = false);
 cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const DefectCfg& cfg,
                                  DefectWorkspace ws, int32_t* flags_out, cudaStream_t st);
 cudaError_t launch_defect_repair(uint16_t* frames, int batch, const DefectCfg& cfg,
@@ -90,6 +106,7 @@ struct AttenuationCfg {
    int wpr;
    int quirk;
    int modules;           // raw layout, see raw_offset
+   int* err = nullptr;    // device error flag of bounded waits (the bulk-copy path needs it)
 };
 // With runs != nullptr the defect repair of each frame is applied on the fly.
 cudaError_t launch_attenuation(const uint16_t* raw, float* out, int batch,
@@ -170,6 +187,18 @@ struct FilterCfg {
 // Empty for lengths the path does not cover.
 std::vector<float2> filter_pass_twiddles(int len);
 cudaError_t launch_filter(float* sino, int batch, const FilterCfg& cfg, cudaStream_t st);
+// Destination of the fused filter + backprojection staging pass: the padded
+// pair sinogram of a staged backprojection variant with S slices per group
+// (window bins u = k + win_lo, u in [0, wp)).
+struct PairsOut {
+   void* pairs;  // float4 records
+   int S, win_lo, wp;
+};
+bool filter_pairs_supported(const FilterCfg& cfg);
+// Filters `batch` slices of sino (not modified) straight into po's pair
+// records; cudaErrorNotSupported for lengths without the radix-16 path.
+cudaError_t launch_filter_pairs(const float* sino, int batch, const FilterCfg& cfg, const PairsOut& po,
+                                cudaStream_t st);
 // Gradient of a loss with respect to the filter taps: the circular
 // cross-correlation of g (gradient at the filter output) with x (filter input)
 // summed over rows, at lag (j - center) mod len for tap j. workspace:
@@ -201,6 +230,9 @@ struct BPCfg {
    // host side only: recorded on the stream after the staging pass and before
    // the backprojection kernel (timing of the two separately)
    cudaEvent_t mid_event = nullptr;
+   bool prefilled = false;  // staged variants: the pair records are already written (launch_filter_pairs)
+   void* adj_scratch = nullptr;  // adjoint: slice-interleaved image copies (bp_adjoint_scratch_bytes)
+   size_t adj_scratch_bytes = 0;
    // adjoint: FP64 line starts split as (hi, lo) floats, [Pp][N]:
    // rowbase = t0 + y * b (walks along x), colbase = t0 + x * a (walks along y)
    const float2* rowbase = nullptr;
@@ -213,6 +245,8 @@ const char* bp_variant_name(int v);
 // Device bytes of the pair sinogram that `variant` needs for `batch` slices
 // (0 for variants that stage windows from the sinogram itself).
 size_t bp_pairs_bytes(int variant, int batch, int Pp, int win_len);
+// Slices per group of a staged variant (the S of its pair records), 0 for the others.
+int bp_variant_pair_slices(int variant);
 // Padding of the pair sinogram: the bin range covering every window that a
 // 32 x 32 tile of the image requests (only tiles meeting the inscribed circle
 // when `masking`), computed with the kernel's own arithmetic.
@@ -222,6 +256,9 @@ cudaError_t launch_backprojection(const float* sino, float* img, int batch, cons
                                   int variant, cudaStream_t st);
 cudaError_t launch_backprojection_adjoint(const float* img, float* sino, int batch,
                                           const BPCfg& cfg, cudaStream_t st);
+// Scratch of the adjoint's fast path for `batch` slices of N x N (without it,
+// the adjoint gathers straight from the image, slowly for steep angles).
+size_t bp_adjoint_scratch_bytes(int batch, int N);
 
 // ---------------------------------------------------------------- masking
 cudaError_t launch_mask(float* img, int batch, int N, float value, int normalize,

@@ -49,6 +49,7 @@ class FBPFunction(torch.autograd.Function):
         n, Pp, Dp = s.shape
         filt = rg.Filter(geom, params, taps=h.detach().cpu().numpy())
         bp = rg.Backprojection(geom, params)
+        bp.reserve_adjoint(chunk)
         gs = torch.empty_like(s)
         gh = torch.zeros(h.shape[0], dtype=torch.float64, device=s.device)
         part = torch.empty(h.shape[0], dtype=torch.float32, device=s.device)
