@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <type_traits>
+
 #include "async_copy.h"
 #include "kernels.h"
 #include "risa_gb300.h"
@@ -546,14 +548,34 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
    const uint32_t wbase = async::smem_u32(wsm);
    const unsigned wmax = (unsigned)(wlen - 1);
    const unsigned long long magic2 = f2_pack(kMagic, kMagic);
+   // Bit r: the warp's 8 x 4 pixel block of step r has a pixel inside the
+   // circle (or no mask is fused). Blocks entirely outside are not
+   // backprojected -- the epilogue writes the mask value there -- which
+   // removes their shared-memory loads in tiles the circle's edge crosses.
+   // The test is the epilogue's (exact in FP32 for N <= 4096: integer
+   // squares below 2^24).
+   unsigned live = (1u << PPT) - 1u;
+   if (cfg.masking) {
+      live = 0u;
+      const int xa = x0 + (warp & 3) * 8;
+      const float nx = fminf(fmaxf(c, (float)xa), (float)(xa + 7)) - c;
+#pragma unroll
+      for (int r = 0; r < PPT; ++r) {
+         const int ya = y0 + (warp >> 2) * 4 + RS * r;
+         const float ny = fminf(fmaxf(c, (float)ya), (float)(ya + 3)) - c;
+         if (nx * nx + ny * ny <= lim) live |= 1u << r;
+      }
+   }
 
    for (int ch = 0; ch < nchunks; ++ch) {
       const int st = ch & 1;
       if (!async::mbar_wait(&full[st], (uint32_t)((ch >> 1) & 1), cfg.err, 5)) s_fail = 1;
-      const int na = min(ACH, Pp - ch * ACH);
+      const int na = live ? min(ACH, Pp - ch * ACH) : 0;
       const uint32_t sbase = wbase + (uint32_t)(st * ACH * H) * plane_bytes;
-#pragma unroll 2
-      for (int ai = 0; ai < na; ++ai) {
+      // one angle of the chunk; CHECK: skip the pixel steps whose block is
+      // outside the circle (warp-uniform), otherwise straight-line code
+      auto angle = [&](int ai, auto check) {
+         constexpr bool CHECK = decltype(check)::value;
          const float a = s_a[st][ai], b = s_b[st][ai];
          const float t0 = s_rel[st][ai] + (float)xo * a + (float)yo * b;
          const float step = (float)RS * b;
@@ -563,16 +585,18 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
             const unsigned long long step2 = f2_pack(step, step);
 #pragma unroll
             for (int r = 0; r < PPT; ++r) {
-               const unsigned long long v2 = f2_add(tm2, magic2);
-               const unsigned long long f2 = f2_sub(tm2, f2_sub(v2, magic2));  // (f, f)
-               float vlo, vhi;
-               f2_unpack(v2, vlo, vhi);
-               const unsigned k = min((unsigned)(__float_as_int(vlo) - kMagicBits), wmax);
-               const uint32_t addr = abase + k * (uint32_t)sizeof(float4);
+               if (!CHECK || (live & (1u << r))) {
+                  const unsigned long long v2 = f2_add(tm2, magic2);
+                  const unsigned long long f2 = f2_sub(tm2, f2_sub(v2, magic2));  // (f, f)
+                  float vlo, vhi;
+                  f2_unpack(v2, vlo, vhi);
+                  const unsigned k = min((unsigned)(__float_as_int(vlo) - kMagicBits), wmax);
+                  const uint32_t addr = abase + k * (uint32_t)sizeof(float4);
 #pragma unroll
-               for (int h = 0; h < H; ++h) {
-                  const ulonglong2 p = lds128_pairs(addr + (uint32_t)h * plane_bytes);
-                  acc2[h][r] = f2_fma(f2, p.y, f2_add(acc2[h][r], p.x));
+                  for (int h = 0; h < H; ++h) {
+                     const ulonglong2 p = lds128_pairs(addr + (uint32_t)h * plane_bytes);
+                     acc2[h][r] = f2_fma(f2, p.y, f2_add(acc2[h][r], p.x));
+                  }
                }
                tm2 = f2_add(tm2, step2);
             }
@@ -580,19 +604,27 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
             float tm = t0;
 #pragma unroll
             for (int r = 0; r < PPT; ++r) {
-               const float v = tm + kMagic;
-               const float f = tm - (v - kMagic);
-               const unsigned k = min((unsigned)(__float_as_int(v) - kMagicBits), wmax);
-               const uint32_t addr = abase + k * (uint32_t)sizeof(float4);
+               if (!CHECK || (live & (1u << r))) {
+                  const float v = tm + kMagic;
+                  const float f = tm - (v - kMagic);
+                  const unsigned k = min((unsigned)(__float_as_int(v) - kMagicBits), wmax);
+                  const uint32_t addr = abase + k * (uint32_t)sizeof(float4);
 #pragma unroll
-               for (int h = 0; h < H; ++h) {
-                  const float4 p = lds128(addr + (uint32_t)h * plane_bytes);
-                  acc[2 * h][r] = fmaf(f, p.z, acc[2 * h][r] + p.x);
-                  acc[2 * h + 1][r] = fmaf(f, p.w, acc[2 * h + 1][r] + p.y);
+                  for (int h = 0; h < H; ++h) {
+                     const float4 p = lds128(addr + (uint32_t)h * plane_bytes);
+                     acc[2 * h][r] = fmaf(f, p.z, acc[2 * h][r] + p.x);
+                     acc[2 * h + 1][r] = fmaf(f, p.w, acc[2 * h + 1][r] + p.y);
+                  }
                }
                tm += step;
             }
          }
+      };
+      if (live == (1u << PPT) - 1u) {
+#pragma unroll 2
+         for (int ai = 0; ai < na; ++ai) angle(ai, std::false_type{});
+      } else {
+         for (int ai = 0; ai < na; ++ai) angle(ai, std::true_type{});
       }
       __syncthreads();
       if (s_fail) {

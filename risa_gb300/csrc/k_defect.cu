@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kStatThreads) defect_stats(const uint16_t* __r
 // packed 16-bit pairs and their total variation in 32 bits (at most
 // kStatRowsVec * 65535 per chunk), and adds the chunk's results atomically.
 // Rows are loaded kStatBatch at a time so that many loads are in flight.
-constexpr int kStatRowsVec = 32;
+constexpr int kStatRowsVec = 64;
 constexpr int kStatBatch = 8;
 __global__ void __launch_bounds__(256) defect_stats_vec8(const uint16_t* __restrict__ frames,
                                                          ColStats* __restrict__ st, int P, int D) {

@@ -217,6 +217,190 @@ __global__ void __launch_bounds__(128, 1) toeplitz_gemm(const __grid_constant__ 
    }
 }
 
+// ---- persistent form -------------------------------------------------------
+// One CTA per SM walks the output tiles t = blockIdx.x, blockIdx.x + gridDim.x,
+// ... in (m block, n block) order, n fastest, so the CTAs working on one m
+// block at a time share its X tiles through L2. Tiles are 128 x 256
+// (tcgen05.mma M128 N256 K16, half the A-tile traffic per flop of the 128 x 128
+// form); K runs in 64-wide blocks through kPStages shared-memory stages. The
+// accumulator is double-buffered in tensor memory (2 x 256 of the 512
+// columns), so the epilogue of one tile runs while the next one is multiplied.
+// Warp roles: 0 TMA producer, 1 MMA issuer (one lane each), 2..5 epilogue
+// (warp w reads TMEM lanes 32 (w % 4) .. 32 (w % 4) + 31). Every wait is
+// bounded; a role that gives up records its code in err and stops, the MMA
+// issuer waits (bounded) for its issued MMAs before the columns are freed.
+constexpr int kPBN = 256, kPStages = 2;
+constexpr int kPTileA = kBM * kBK * 2;                     // 16 KiB
+constexpr int kPTileB = kPBN * kBK * 2;                    // 32 KiB
+constexpr int kPStageBytes = 2 * kPTileA + 2 * kPTileB;    // 96 KiB: Xh, Xl, Th, Tl
+constexpr uint32_t kPTmemCols = 512;
+constexpr uint32_t kIdescBf16P = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kPBN >> 3) << 17) |
+                                 ((uint32_t)(kBM >> 4) << 24);
+constexpr uint32_t kIdescF16P = (1u << 4) | ((uint32_t)(kPBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(192, 1) toeplitz_gemm_persistent(const __grid_constant__ CUtensorMap map_xh,
+                                                                   const __grid_constant__ CUtensorMap map_xl,
+                                                                   const __grid_constant__ CUtensorMap map_th,
+                                                                   const __grid_constant__ CUtensorMap map_tl,
+                                                                   float* __restrict__ y, int M, int N, int K,
+                                                                   int* __restrict__ err, uint32_t idesc,
+                                                                   const float* __restrict__ row_inv, float t_inv) {
+   extern __shared__ __align__(1024) unsigned char smem_raw[];
+   unsigned char* smem = reinterpret_cast<unsigned char*>(
+       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+   __shared__ __align__(8) uint64_t full_bar[kPStages], empty_bar[kPStages], tfull[2], tempty[2], drain_bar;
+   __shared__ uint32_t tmem_base_slot;
+   __shared__ volatile int cta_failed;
+
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int nblocks = N / kPBN, mblocks = (M + kBM - 1) / kBM;
+   const int tiles = nblocks * mblocks;
+   const int kblocks = K / kBK;
+
+   if (threadIdx.x == 0) {
+      for (int s = 0; s < kPStages; ++s) {
+         mbar_init(&full_bar[s], 1);
+         mbar_init(&empty_bar[s], 1);
+      }
+      for (int b = 0; b < 2; ++b) {
+         mbar_init(&tfull[b], 1);
+         mbar_init(&tempty[b], 4);  // one arrival per epilogue warp
+      }
+      mbar_init(&drain_bar, 1);
+      cta_failed = 0;
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+   }
+   if (warp == 1) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       smem_u32(&tmem_base_slot)),
+                   "r"(kPTmemCols)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   const uint32_t tmem_d = tmem_base_slot;
+
+   if (warp == 0) {
+      if (lane == 0) {
+         uint32_t g = 0;  // k blocks loaded so far
+         bool ok = true;
+         for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+            const int m0 = (t / nblocks) * kBM, n0 = (t % nblocks) * kPBN;
+            for (int kb = 0; kb < kblocks; ++kb, ++g) {
+               const int s = (int)(g % kPStages);
+               const uint32_t ph = (g / kPStages) & 1u;
+               if (cta_failed || !mbar_wait(&empty_bar[s], ph ^ 1u, err, 1)) {
+                  ok = false;
+                  break;
+               }
+               unsigned char* st = smem + (size_t)s * kPStageBytes;
+               mbar_arrive_expect_tx(&full_bar[s], kPStageBytes);
+               const int kx = kb * kBK;  // 64 16-bit values = 128 bytes: 16-byte aligned
+               tma_load_2d(st, &map_xh, &full_bar[s], kx, m0);
+               tma_load_2d(st + kPTileA, &map_xl, &full_bar[s], kx, m0);
+               tma_load_2d(st + 2 * kPTileA, &map_th, &full_bar[s], kx, n0);
+               tma_load_2d(st + 2 * kPTileA + kPTileB, &map_tl, &full_bar[s], kx, n0);
+            }
+         }
+         if (!ok) {
+            cta_failed = 1;
+            // the last stages armed may still be landing: let them finish
+            for (int s = 0; s < kPStages; ++s) {
+               const uint32_t last = g > (uint32_t)s ? (g - 1u - (uint32_t)((g - 1u - s) % kPStages)) : 0u;
+               if (g > (uint32_t)s) async::mbar_wait_quiet(&full_bar[s], (last / kPStages) & 1u);
+            }
+         }
+      }
+      __syncwarp();
+   } else if (warp == 1) {
+      if (lane == 0) {
+         uint32_t g = 0, i = 0;
+         bool ok = true;
+         for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
+            const int b = (int)(i & 1u);
+            const uint32_t tph = (i >> 1) & 1u;
+            if (cta_failed || !mbar_wait(&tempty[b], tph ^ 1u, err, 4)) {
+               ok = false;
+               break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t d = tmem_d + (uint32_t)(b * kPBN);
+            for (int kb = 0; kb < kblocks; ++kb, ++g) {
+               const int s = (int)(g % kPStages);
+               const uint32_t ph = (g / kPStages) & 1u;
+               if (!mbar_wait(&full_bar[s], ph, err, 2)) {
+                  ok = false;
+                  break;
+               }
+               asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+               unsigned char* st = smem + (size_t)s * kPStageBytes;
+               const uint64_t dxh = smem_desc(st), dxl = smem_desc(st + kPTileA);
+               const uint64_t dth = smem_desc(st + 2 * kPTileA), dtl = smem_desc(st + 2 * kPTileA + kPTileB);
+#pragma unroll
+               for (int kk = 0; kk < kBK / 16; ++kk) {
+                  const uint64_t o = (uint64_t)((kk * 32) >> 4);  // 16 values = 32 bytes along K
+                  const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+                  umma_f16(d, dxh + o, dth + o, idesc, acc0);
+                  umma_f16(d, dxh + o, dtl + o, idesc, 1u);
+                  umma_f16(d, dxl + o, dth + o, idesc, 1u);
+               }
+               umma_commit(&empty_bar[s]);  // the stage is free once these MMAs finish
+            }
+            if (!ok) break;
+            umma_commit(&tfull[b]);  // the tile's accumulator is complete
+         }
+         if (!ok) cta_failed = 1;
+         umma_commit(&drain_bar);  // arrives when every MMA issued above has finished
+         async::mbar_wait_quiet(&drain_bar, 0);
+      }
+      __syncwarp();
+   } else {
+      const int q = warp & 3;  // TMEM lane quarter of this warp
+      uint32_t i = 0;
+      for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+         const int b = (int)(i & 1u);
+         const uint32_t tph = (i >> 1) & 1u;
+         if (cta_failed || !mbar_wait(&tfull[b], tph, err, 3)) {
+            cta_failed = 1;
+            break;
+         }
+         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+         const int m0 = (t / nblocks) * kBM, n0 = (t % nblocks) * kPBN;
+         const int row = m0 + q * 32 + lane;
+         // power-of-two scales of the fp16 form: exact
+         const float sc = row_inv ? (row < M ? row_inv[row] : 0.f) * t_inv : t_inv;
+#pragma unroll 1
+         for (int c = 0; c < kPBN; c += 32) {
+            uint32_t r[32];
+            tmem_ld32(tmem_d + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kPBN + c), r);
+            if (row < M) {
+               float4* dst = reinterpret_cast<float4*>(y + (size_t)row * N + n0 + c);
+#pragma unroll
+               for (int v = 0; v < 8; ++v)
+                  dst[v] = make_float4(__uint_as_float(r[4 * v]) * sc, __uint_as_float(r[4 * v + 1]) * sc,
+                                       __uint_as_float(r[4 * v + 2]) * sc, __uint_as_float(r[4 * v + 3]) * sc);
+            }
+         }
+         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+         __syncwarp();
+         if (lane == 0) mbar_arrive(&tempty[b]);  // the MMA issuer may overwrite this buffer
+      }
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   if (warp == 1) {
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_d), "r"(kPTmemCols)
+                   : "memory");
+   }
+}
+
 // fp32 rows -> bf16 (hi, lo) with hi = rn(x), lo = rn(x - hi)
 __global__ void split_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict__ hi,
                            __nv_bfloat16* __restrict__ lo, size_t n) {
@@ -267,13 +451,13 @@ EncodeTiled encode_fn() {
    return fn;
 }
 
-// 16-bit matrix [rows][cols] (cols contiguous), boxes of 64 columns x 128 rows.
-bool make_map(CUtensorMap* map, const void* base, int rows, int cols, bool f16) {
+// 16-bit matrix [rows][cols] (cols contiguous), boxes of 64 columns x box_rows rows.
+bool make_map(CUtensorMap* map, const void* base, int rows, int cols, bool f16, int box_rows = kBM) {
    EncodeTiled enc = encode_fn();
    if (!enc) return false;
    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
    const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
-   const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+   const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
    const cuuint32_t estr[2] = {1, 1};
    return enc(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -281,7 +465,10 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int cols, bool f16) 
 }
 }  // namespace
 
-size_t toeplitz_smem_bytes() { return (size_t)kStages * kStageBytes + 1024; }
+size_t toeplitz_smem_bytes() {
+   const size_t a = (size_t)kStages * kStageBytes, b = (size_t)kPStages * kPStageBytes;
+   return (a > b ? a : b) + 1024;
+}
 
 cudaError_t launch_toeplitz(const ToeplitzArgs& a, cudaStream_t st) {
    if (a.rows <= 0) return cudaSuccess;
@@ -297,6 +484,23 @@ cudaError_t launch_toeplitz(const ToeplitzArgs& a, cudaStream_t st) {
                                                              static_cast<__nv_bfloat16*>(a.xl), n);
    }
    CUtensorMap mxh, mxl, mth, mtl;
+   if (a.n % kPBN == 0) {  // persistent 128 x 256 tiles
+      if (!make_map(&mxh, a.xh, a.rows, a.k, f16) || !make_map(&mxl, a.xl, a.rows, a.k, f16) ||
+          !make_map(&mth, a.th, a.n, a.k, f16, kPBN) || !make_map(&mtl, a.tl, a.n, a.k, f16, kPBN))
+         return cudaErrorInvalidValue;
+      const size_t smem = (size_t)kPStages * kPStageBytes + 1024;
+      cudaError_t e =
+          cudaFuncSetAttribute(toeplitz_gemm_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      int dev = 0, sms = 0;
+      if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+      const int tiles = (a.n / kPBN) * ((a.rows + kBM - 1) / kBM);
+      toeplitz_gemm_persistent<<<tiles < sms ? tiles : sms, 192, smem, st>>>(
+          mxh, mxl, mth, mtl, a.y, a.rows, a.n, a.k, a.err, f16 ? kIdescF16P : kIdescBf16P,
+          f16 ? a.row_inv : nullptr, a.t_inv);
+      return cudaGetLastError();
+   }
    if (!make_map(&mxh, a.xh, a.rows, a.k, f16) || !make_map(&mxl, a.xl, a.rows, a.k, f16) ||
        !make_map(&mth, a.th, a.n, a.k, f16) || !make_map(&mtl, a.tl, a.n, a.k, f16))
       return cudaErrorInvalidValue;

@@ -46,6 +46,10 @@ def _run(Pp, Dp, pad, ftype, batch, seed, split=rg.SPLIT_BF16X3):
         mf, _ = rel_err(got_f[b], exp)
         assert mf < 1e-5, mf
         assert mt < bar, (split, mt)
+    # every slice (all tiles of the persistent kernel's later rounds) against the FFT form
+    for b in range(batch):
+        mt, _ = rel_err(got_t[b], got_f[b])
+        assert mt < bar + 1e-5, (split, b, mt)
 
 
 def test_toeplitz_small_with_ragged_rows():
@@ -59,3 +63,10 @@ def test_toeplitz_precision_geometry():
 def test_toeplitz_f16_split():
     _run(Pp=100, Dp=128, pad=256, ftype="ramp", batch=3, seed=3, split=rg.SPLIT_F16X3)
     _run(Pp=1024, Dp=1024, pad=2048, ftype="sheppLogan", batch=2, seed=4, split=rg.SPLIT_F16X3)
+
+
+def test_toeplitz_persistent_many_tiles():
+    # 40000 rows x 512 outputs: 313 x 2 tiles of 128 x 256, several per CTA
+    # (both accumulator buffers and stage phases wrap many times), last m block partial
+    _run(Pp=1000, Dp=512, pad=1024, ftype="hanning", batch=40, seed=5)
+    _run(Pp=1000, Dp=512, pad=1024, ftype="ramp", batch=40, seed=6, split=rg.SPLIT_F16X3)
