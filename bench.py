@@ -484,7 +484,7 @@ def measure_precision(torch, rg, dev):
         if name.startswith("toeplitz"):
             rec["useful_tflops"] = useful / (ms / 1e3) / 1e12
             rec["executed_tflops"] = 3 * useful / (ms / 1e3) / 1e12
-            kind = "fp16 (power-of-two scaled)" if "f16" in name else "bf16"
+            kind = "fp16 (power-of-two scaled)" if name.endswith("_f16x3") else "bf16"
             rec["gemm"] = f"M = {S * Pp} rows, K = N = {Dp} (zero padding not computed), 3 {kind} products"
         out[name] = rec
     return out

@@ -176,20 +176,26 @@ __device__ __forceinline__ void r16_filter_core(float2 (&v)[16], float2* buf, in
    r16_load<LEN, P::R3>(buf, lt, v);
    __syncthreads();
    r16_compute<LEN, P::R3, P::NS3>(lt, v, tw3);
-   // spectrum index of v[b R3 + r] equals r16_time_index; filter and conjugate
+   // Spectrum index of v[b R3 + r] is r16_time_index = lt + (LEN/16) m with
+   // m = b + out_slot(r) (16/R3), and LEN = 16 R2 R3 makes m run over 0..15:
+   // a thread holds exactly the 16 values the first inverse pass reads
+   // (z[lt + m LEN/16] in slot m). Filter, conjugate and renumber the
+   // registers -- no shared-memory exchange between the transforms.
+   {
+      float2 w[16];
 #pragma unroll
-   for (int b = 0; b < 16 / P::R3; ++b)
+      for (int b = 0; b < 16 / P::R3; ++b)
 #pragma unroll
-      for (int r = 0; r < P::R3; ++r) {
-         const int idx = r16_time_index<LEN>(lt, b, r);
-         float2 hh = __ldg(h + idx);
-         if (adjoint) hh.y = -hh.y;
-         const float2 y = cmul(v[b * P::R3 + r], hh);
-         buf[pad16(idx)] = make_float2(y.x, -y.y);
-      }
-   __syncthreads();
-   r16_load<LEN, 16>(buf, lt, v);
-   __syncthreads();
+         for (int r = 0; r < P::R3; ++r) {
+            const int idx = r16_time_index<LEN>(lt, b, r);
+            float2 hh = __ldg(h + idx);
+            if (adjoint) hh.y = -hh.y;
+            const float2 y = cmul(v[b * P::R3 + r], hh);
+            w[b + out_slot<P::R3>(r) * (16 / P::R3)] = make_float2(y.x, -y.y);
+         }
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[m] = w[m];
+   }
    r16_compute<LEN, 16, 1>(lt, v, nullptr);
    r16_store<LEN, 16, 1>(buf, lt, v);
    __syncthreads();

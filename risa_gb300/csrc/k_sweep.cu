@@ -10,6 +10,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <type_traits>
+
 #include "async_copy.h"
 #include "fft_r16.cuh"
 #include "kernels.h"
@@ -204,26 +206,48 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
       const uint32_t wbase = async::smem_u32(wsm);
       const unsigned wmax = (unsigned)(W - 1);
       bool failed = false;
+      // Bit r: the warp's 8 x 4 pixel block of step r lies (partly) in the
+      // image and, with the mask, (partly) inside the circle; other blocks
+      // are not backprojected (exact test, as in the epilogue).
+      unsigned live = 0u;
+      {
+         const int xa = x0 + (warp & 3) * 8;
+         const float nx = fminf(fmaxf(c, (float)xa), (float)(xa + 7)) - c;
+#pragma unroll
+         for (int r = 0; r < PPT; ++r) {
+            const int ya = y0 + (warp >> 2) * 4 + RS * r;
+            const float ny = fminf(fmaxf(c, (float)ya), (float)(ya + 3)) - c;
+            if (xa < N && ya < N && (!I.masking || nx * nx + ny * ny <= lim)) live |= 1u << r;
+         }
+      }
       for (int ch = 0; ch < nchunks; ++ch) {
          const int st = ch & 1;
          if (!async::mbar_wait(&full[st], uses[st] & 1u, A.err, 5)) S.fail = 1;
          ++uses[st];
-         const int na = min(kSweepACH, Pp - ch * kSweepACH);
-#pragma unroll 2
-         for (int ai = 0; ai < na; ++ai) {
+         const int na = live ? min(kSweepACH, Pp - ch * kSweepACH) : 0;
+         auto angle = [&](int ai, auto check) {
+            constexpr bool CHECK = decltype(check)::value;
             const float a = S.a[st][ai], b = S.b[st][ai];
             float tm = S.rel[st][ai] + (float)xo * a + (float)yo * b;
             const float step = (float)RS * b;
             const uint32_t abase = wbase + (uint32_t)((st * kSweepACH + ai) * W) * (uint32_t)sizeof(float2);
 #pragma unroll
             for (int r = 0; r < PPT; ++r) {
-               const float v = tm + kSweepMagic;
-               const float f = tm - (v - kSweepMagic);
-               const unsigned k = min((unsigned)(__float_as_int(v) - kSweepMagicBits), wmax);
-               const float2 p = lds64(abase + k * (uint32_t)sizeof(float2));
-               acc[r] = fmaf(f, p.y, acc[r] + p.x);
+               if (!CHECK || (live & (1u << r))) {
+                  const float v = tm + kSweepMagic;
+                  const float f = tm - (v - kSweepMagic);
+                  const unsigned k = min((unsigned)(__float_as_int(v) - kSweepMagicBits), wmax);
+                  const float2 p = lds64(abase + k * (uint32_t)sizeof(float2));
+                  acc[r] = fmaf(f, p.y, acc[r] + p.x);
+               }
                tm += step;
             }
+         };
+         if (live == (1u << PPT) - 1u) {
+#pragma unroll 2
+            for (int ai = 0; ai < na; ++ai) angle(ai, std::false_type{});
+         } else {
+            for (int ai = 0; ai < na; ++ai) angle(ai, std::true_type{});
          }
          __syncthreads();
          if (S.fail) {
