@@ -43,7 +43,7 @@ SMEM_BYTES_PER_UPDATE = 8  # one FP32 (midpoint, difference) pair per pixel x an
 SMEM_BYTES_PER_CLK_SM = 128  # nominal shared-memory bandwidth per SM
 # dram__bytes_read.sum + dram__bytes_write.sum of one 64-slice backprojection launch
 # (profiles/bp_staged_fbp512_ncu.txt)
-BP_DRAM_BYTES_PER_LAUNCH = 772.6e6
+BP_DRAM_BYTES_PER_LAUNCH = 724.1e6
 WORKLOAD_NAME = ("full-rate streaming: 2 planes x 2000 frames of 1000x1152 uint16 fan sinograms, 1% defective "
                  "detectors -> 1024x1024 parallel (pad 2048, Shepp-Logan) -> 512^2 FP32, circular mask")
 
@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/roofline/cpu legs")
     ap.add_argument("--bp-variant", type=int, default=-1,
                     help="backprojection variant to use instead of autotuning (for profiling one kernel)")
+    ap.add_argument("--only", choices=["precision", "differentiation", "sweep"], default=None,
+                    help="run one of the other scope-table workloads alone and print its JSON (no headline)")
     return ap.parse_args()
 
 
@@ -599,6 +601,17 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.only:
+        import torch
+
+        import risa_gb300 as rg
+
+        dev = torch.device("cuda", local_rank)
+        torch.cuda.set_device(dev)
+        fn = {"precision": measure_precision, "differentiation": measure_differentiation,
+              "sweep": measure_sweep}[args.only]
+        print(json.dumps({"workload": args.only, **fn(torch, rg, dev)}), flush=True)
         return
     if world > 1:
         import torch

@@ -47,6 +47,10 @@ constexpr BPVariant kVariants[] = {
     {kAsyncPacked, 4, 16, 4, "staged_f32x2_s4_a16_p4"},
     {kAsyncPacked, 2, 16, 8, "staged_f32x2_s2_a16_p8"},
     {kAsyncPacked, 4, 8, 8, "staged_f32x2_s4_a8_p8"},
+    {kAsync, 4, 16, 4, "staged_s4_a16_p4"},
+    {kAsync, 4, 4, 4, "staged_s4_a4_p4"},
+    {kAsync, 2, 8, 4, "staged_s2_a8_p4"},
+    {kAsync, 4, 16, 8, "staged_s4_a16_p8"},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 

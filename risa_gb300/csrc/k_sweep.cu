@@ -10,8 +10,6 @@
 #include <algorithm>
 #include <cmath>
 
-#include <type_traits>
-
 #include "async_copy.h"
 #include "fft_r16.cuh"
 #include "kernels.h"
@@ -207,8 +205,10 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
       const unsigned wmax = (unsigned)(W - 1);
       bool failed = false;
       // Bit r: the warp's 8 x 4 pixel block of step r lies (partly) in the
-      // image and, with the mask, (partly) inside the circle; other blocks
-      // are not backprojected (exact test, as in the epilogue).
+      // image and, with the mask, (partly) inside the circle (exact test, as
+      // in the epilogue). A warp with no such block skips the angle loop; the
+      // others run it in full -- this loop is issue-bound, and a per-block
+      // branch costs more than the shared-memory loads it would save.
       unsigned live = 0u;
       {
          const int xa = x0 + (warp & 3) * 8;
@@ -225,29 +225,21 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
          if (!async::mbar_wait(&full[st], uses[st] & 1u, A.err, 5)) S.fail = 1;
          ++uses[st];
          const int na = live ? min(kSweepACH, Pp - ch * kSweepACH) : 0;
-         auto angle = [&](int ai, auto check) {
-            constexpr bool CHECK = decltype(check)::value;
+#pragma unroll 2
+         for (int ai = 0; ai < na; ++ai) {
             const float a = S.a[st][ai], b = S.b[st][ai];
             float tm = S.rel[st][ai] + (float)xo * a + (float)yo * b;
             const float step = (float)RS * b;
             const uint32_t abase = wbase + (uint32_t)((st * kSweepACH + ai) * W) * (uint32_t)sizeof(float2);
 #pragma unroll
             for (int r = 0; r < PPT; ++r) {
-               if (!CHECK || (live & (1u << r))) {
-                  const float v = tm + kSweepMagic;
-                  const float f = tm - (v - kSweepMagic);
-                  const unsigned k = min((unsigned)(__float_as_int(v) - kSweepMagicBits), wmax);
-                  const float2 p = lds64(abase + k * (uint32_t)sizeof(float2));
-                  acc[r] = fmaf(f, p.y, acc[r] + p.x);
-               }
+               const float v = tm + kSweepMagic;
+               const float f = tm - (v - kSweepMagic);
+               const unsigned k = min((unsigned)(__float_as_int(v) - kSweepMagicBits), wmax);
+               const float2 p = lds64(abase + k * (uint32_t)sizeof(float2));
+               acc[r] = fmaf(f, p.y, acc[r] + p.x);
                tm += step;
             }
-         };
-         if (live == (1u << PPT) - 1u) {
-#pragma unroll 2
-            for (int ai = 0; ai < na; ++ai) angle(ai, std::false_type{});
-         } else {
-            for (int ai = 0; ai < na; ++ai) angle(ai, std::true_type{});
          }
          __syncthreads();
          if (S.fail) {
