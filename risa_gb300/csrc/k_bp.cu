@@ -467,7 +467,10 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
    constexpr int T = 32, H = S / 2, NT = 1024 / PPT, RS = NT / 32;  // RS: rows between a thread's pixels
    extern __shared__ float4 wsm[];  // [2][ACH][H][wlen]
    __shared__ uint64_t full[2];
-   __shared__ float s_a[2][ACH], s_b[2][ACH], s_rel[2][ACH];
+   // per angle of a chunk: (a, b, window-relative coordinate, unused), read
+   // with one broadcast 16-byte load per angle (three 4-byte loads cost 8% of
+   // the shared-memory wavefronts of the backprojection)
+   __shared__ float4 s_par[2][ACH];
    __shared__ int s_fail;
 
    const int N = cfg.N, Pp = cfg.Pp;
@@ -517,9 +520,7 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
             atomicCAS(cfg.err, 0, 4);
             u0 = min(max(u0, 0), wp - wlen);
          }
-         s_a[st][lane] = a;
-         s_b[st][lane] = b;
-         s_rel[st][lane] = (float)(base - (double)w0 - 0.5);
+         s_par[st][lane] = make_float4(a, b, (float)(base - (double)w0 - 0.5), 0.f);
 #pragma unroll
          for (int h = 0; h < H; ++h)
             async::bulk_load(wsm + ((size_t)(st * ACH + lane) * H + h) * wlen,
@@ -580,8 +581,9 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
       // outside the circle (warp-uniform), otherwise straight-line code
       auto angle = [&](int ai, auto check) {
          constexpr bool CHECK = decltype(check)::value;
-         const float a = s_a[st][ai], b = s_b[st][ai];
-         const float t0 = s_rel[st][ai] + (float)xo * a + (float)yo * b;
+         const float4 q = s_par[st][ai];
+         const float a = q.x, b = q.y;
+         const float t0 = q.z + (float)xo * a + (float)yo * b;
          const float step = (float)RS * b;
          const uint32_t abase = sbase + (uint32_t)(ai * H) * plane_bytes;
          if (PACKED) {

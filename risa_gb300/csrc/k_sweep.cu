@@ -115,7 +115,7 @@ __device__ void sweep_rows(const SweepArgs& A, const SweepInst& I, int index, fl
 }
 
 struct TileShared {
-   float a[2][kSweepACH], b[2][kSweepACH], rel[2][kSweepACH];
+   float4 par[2][kSweepACH];  // per angle of a chunk: (a, b, window-relative coordinate, unused)
    int ok, fail;
 };
 
@@ -185,9 +185,7 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
                atomicCAS(A.err, 0, 4);
                u0 = min(max(u0, 0), I.win_len - W) & ~1;
             }
-            S.a[st][lane] = a;
-            S.b[st][lane] = b;
-            S.rel[st][lane] = (float)(base - (double)w0 - 0.5);
+            S.par[st][lane] = make_float4(a, b, (float)(base - (double)w0 - 0.5), 0.f);
             async::bulk_load(wsm + (size_t)(st * kSweepACH + lane) * W, prow + (size_t)ang * I.win_len + u0,
                              win_bytes, &full[st]);
          }
@@ -227,8 +225,9 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
          const int na = live ? min(kSweepACH, Pp - ch * kSweepACH) : 0;
 #pragma unroll 2
          for (int ai = 0; ai < na; ++ai) {
-            const float a = S.a[st][ai], b = S.b[st][ai];
-            float tm = S.rel[st][ai] + (float)xo * a + (float)yo * b;
+            const float4 q = S.par[st][ai];  // one broadcast load per angle
+            const float a = q.x, b = q.y;
+            float tm = q.z + (float)xo * a + (float)yo * b;
             const float step = (float)RS * b;
             const uint32_t abase = wbase + (uint32_t)((st * kSweepACH + ai) * W) * (uint32_t)sizeof(float2);
 #pragma unroll
