@@ -471,7 +471,8 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
    // with one broadcast 16-byte load per angle (three 4-byte loads cost 8% of
    // the shared-memory wavefronts of the backprojection)
    __shared__ float4 s_par[2][ACH];
-   __shared__ int s_fail;
+   __shared__ volatile int s_fail;
+   __shared__ int s_break;
 
    const int N = cfg.N, Pp = cfg.Pp;
    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
@@ -505,11 +506,19 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
    const float4* grow = pairs + (size_t)g * Pp * H * wp;
    const uint32_t plane_bytes = (uint32_t)wlen * (uint32_t)sizeof(float4);
 
-   // warp 0: parameters and bulk copies of chunk ch into stage st
-   auto issue = [&](int ch, int st) {
+   // warp 0: parameters and bulk copies of chunk ch into stage st. The
+   // parameters are stored before lane 0's arrive (a release), so a warp that
+   // sees the stage's phase complete (an acquire) reads them; the copies are
+   // issued after the arrive armed the byte count.
+   // prep: this lane's angle of chunk ch (FP64 window start, parameters);
+   // commit: store the parameters, arm the stage, issue the copies.
+   struct Prep {
+      float4 par;
+      int u0;
+   };
+   auto prep = [&](int ch) {
+      Prep r{make_float4(0.f, 0.f, 0.f, 0.f), 0};
       const int na = min(ACH, Pp - ch * ACH);
-      if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)(na * H) * plane_bytes);
-      __syncwarp();
       if (lane < na) {
          const int ang = ch * ACH + lane;
          const float a = __ldg(cfg.a + ang), b = __ldg(cfg.b + ang);
@@ -520,18 +529,32 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
             atomicCAS(cfg.err, 0, 4);
             u0 = min(max(u0, 0), wp - wlen);
          }
-         s_par[st][lane] = make_float4(a, b, (float)(base - (double)w0 - 0.5), 0.f);
+         r.par = make_float4(a, b, (float)(base - (double)w0 - 0.5), 0.f);
+         r.u0 = u0;
+      }
+      return r;
+   };
+   auto commit = [&](int ch, int st, const Prep& r) {
+      const int na = min(ACH, Pp - ch * ACH);
+      if (lane < na) s_par[st][lane] = r.par;
+      __syncwarp();
+      if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)(na * H) * plane_bytes);
+      __syncwarp();
+      if (lane < na) {
+         const int ang = ch * ACH + lane;
 #pragma unroll
          for (int h = 0; h < H; ++h)
             async::bulk_load(wsm + ((size_t)(st * ACH + lane) * H + h) * wlen,
-                             grow + ((size_t)ang * H + h) * wp + u0, plane_bytes, &full[st]);
+                             grow + ((size_t)ang * H + h) * wp + r.u0, plane_bytes, &full[st]);
       }
    };
+   auto issue = [&](int ch, int st) { commit(ch, st, prep(ch)); };
 
    if (threadIdx.x == 0) {
       async::mbar_init(&full[0], 1);
       async::mbar_init(&full[1], 1);
       s_fail = 0;
+      s_break = nchunks - 1;  // a wait that gives up after warp 0 finished leaves nothing in flight
       async::mbar_init_fence();
    }
    __syncthreads();
@@ -632,16 +655,41 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
       } else {
          for (int ai = 0; ai < na; ++ai) angle(ai, std::true_type{});
       }
-      __syncthreads();
-      if (s_fail) {
-         // drain this CTA's copies still in flight, then leave without output
-         if (threadIdx.x == 0) {
-            async::mbar_wait_quiet(&full[st], (uint32_t)((ch >> 1) & 1));
-            if (ch + 1 < nchunks) async::mbar_wait_quiet(&full[st ^ 1], (uint32_t)(((ch + 1) >> 1) & 1));
-         }
-         return;
+      // Release the stage: the other warps arrive on named barrier 1 + (ch & 1)
+      // without waiting and go on with the next stage; only warp 0 waits for
+      // all of them before refilling this stage with chunk ch + 2. Two barrier
+      // ids keep a warp one chunk ahead from counting towards this one.
+      if (warp == 0) {
+         if (ch & 1)
+            asm volatile("bar.sync 2, %0;" ::"n"(NT) : "memory");
+         else
+            asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
+      } else {
+         if (ch & 1)
+            asm volatile("bar.arrive 2, %0;" ::"n"(NT) : "memory");
+         else
+            asm volatile("bar.arrive 1, %0;" ::"n"(NT) : "memory");
       }
-      if (warp == 0 && ch + 2 < nchunks) issue(ch + 2, st);
+      if (s_fail) {
+         if (warp == 0) s_break = ch;
+         break;
+      }
+      if (warp == 0 && ch + 2 < nchunks) {
+         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+         issue(ch + 2, st);
+      }
+   }
+   __syncthreads();
+   if (s_fail) {
+      // a wait gave up: warp 0 stopped after chunk s_break, so the chunks it
+      // issued that may still be landing are s_break and s_break + 1; let them
+      // land, then leave without output
+      if (threadIdx.x == 0) {
+         const int ch = s_break;
+         async::mbar_wait_quiet(&full[ch & 1], (uint32_t)((ch >> 1) & 1));
+         if (ch + 1 < nchunks) async::mbar_wait_quiet(&full[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1));
+      }
+      return;
    }
    if (PACKED) {
 #pragma unroll
