@@ -460,17 +460,37 @@ __device__ __forceinline__ ulonglong2 lds128_pairs(uint32_t addr) {
    return v;
 }
 
-template <int S, int ACH, bool PACKED, int PPT>
+// Named barrier 1 + id: bar.sync (the refilling warp) or bar.arrive (the others).
+template <int NT>
+__device__ __forceinline__ void stage_barrier(int id, bool wait) {
+   switch (id) {
+#define RG_STAGE_BAR(I)                                                     \
+   case I:                                                                  \
+      if (wait)                                                             \
+         asm volatile("bar.sync " #I ", %0;" ::"n"(NT) : "memory");         \
+      else                                                                  \
+         asm volatile("bar.arrive " #I ", %0;" ::"n"(NT) : "memory");       \
+      break;
+      RG_STAGE_BAR(1)
+      RG_STAGE_BAR(2)
+      RG_STAGE_BAR(3)
+      default: RG_STAGE_BAR(4)
+#undef RG_STAGE_BAR
+   }
+}
+
+template <int S, int ACH, bool PACKED, int PPT, int NST>
 __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __restrict__ pairs,
                                                               float* __restrict__ img, BPCfg cfg, int wlen,
                                                               int batch) {
+   static_assert(NST >= 2 && NST <= 4, "2 to 4 stages (one named barrier each)");
    constexpr int T = 32, H = S / 2, NT = 1024 / PPT, RS = NT / 32;  // RS: rows between a thread's pixels
-   extern __shared__ float4 wsm[];  // [2][ACH][H][wlen]
-   __shared__ uint64_t full[2];
+   extern __shared__ float4 wsm[];  // [NST][ACH][H][wlen]
+   __shared__ uint64_t full[NST];
    // per angle of a chunk: (a, b, window-relative coordinate, unused), read
    // with one broadcast 16-byte load per angle (three 4-byte loads cost 8% of
    // the shared-memory wavefronts of the backprojection)
-   __shared__ float4 s_par[2][ACH];
+   __shared__ float4 s_par[NST][ACH];
    __shared__ volatile int s_fail;
    __shared__ int s_break;
 
@@ -551,17 +571,14 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
    auto issue = [&](int ch, int st) { commit(ch, st, prep(ch)); };
 
    if (threadIdx.x == 0) {
-      async::mbar_init(&full[0], 1);
-      async::mbar_init(&full[1], 1);
+      for (int i = 0; i < NST; ++i) async::mbar_init(&full[i], 1);
       s_fail = 0;
       s_break = nchunks - 1;  // a wait that gives up after warp 0 finished leaves nothing in flight
       async::mbar_init_fence();
    }
    __syncthreads();
-   if (warp == 0) {
-      issue(0, 0);
-      if (nchunks > 1) issue(1, 1);
-   }
+   if (warp == 0)
+      for (int i = 0; i < NST && i < nchunks; ++i) issue(i, i);
    __syncthreads();
 
    float acc[S][PPT];
@@ -596,8 +613,8 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
    }
 
    for (int ch = 0; ch < nchunks; ++ch) {
-      const int st = ch & 1;
-      if (!async::mbar_wait(&full[st], (uint32_t)((ch >> 1) & 1), cfg.err, 5)) s_fail = 1;
+      const int st = ch % NST;
+      if (!async::mbar_wait(&full[st], (uint32_t)((ch / NST) & 1), cfg.err, 5)) s_fail = 1;
       const int na = live ? min(ACH, Pp - ch * ACH) : 0;
       const uint32_t sbase = wbase + (uint32_t)(st * ACH * H) * plane_bytes;
       // one angle of the chunk; CHECK: skip the pixel steps whose block is
@@ -655,40 +672,29 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
       } else {
          for (int ai = 0; ai < na; ++ai) angle(ai, std::true_type{});
       }
-      // Release the stage: the other warps arrive on named barrier 1 + (ch & 1)
-      // without waiting and go on with the next stage; only warp 0 waits for
-      // all of them before refilling this stage with chunk ch + 2. Two barrier
-      // ids keep a warp one chunk ahead from counting towards this one.
-      if (warp == 0) {
-         if (ch & 1)
-            asm volatile("bar.sync 2, %0;" ::"n"(NT) : "memory");
-         else
-            asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
-      } else {
-         if (ch & 1)
-            asm volatile("bar.arrive 2, %0;" ::"n"(NT) : "memory");
-         else
-            asm volatile("bar.arrive 1, %0;" ::"n"(NT) : "memory");
-      }
+      // Release the stage: the other warps arrive on named barrier
+      // 1 + ch % NST without waiting and go on with the stages already
+      // loaded; only warp 0 waits for all of them before refilling this
+      // stage with chunk ch + NST. A warp is at most NST - 1 chunks ahead,
+      // so NST barrier ids keep it from counting towards this chunk.
+      stage_barrier<NT>(1 + ch % NST, warp == 0);
       if (s_fail) {
          if (warp == 0) s_break = ch;
          break;
       }
-      if (warp == 0 && ch + 2 < nchunks) {
+      if (warp == 0 && ch + NST < nchunks) {
          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-         issue(ch + 2, st);
+         issue(ch + NST, st);
       }
    }
    __syncthreads();
    if (s_fail) {
       // a wait gave up: warp 0 stopped after chunk s_break, so the chunks it
-      // issued that may still be landing are s_break and s_break + 1; let them
-      // land, then leave without output
-      if (threadIdx.x == 0) {
-         const int ch = s_break;
-         async::mbar_wait_quiet(&full[ch & 1], (uint32_t)((ch >> 1) & 1));
-         if (ch + 1 < nchunks) async::mbar_wait_quiet(&full[(ch + 1) & 1], (uint32_t)(((ch + 1) >> 1) & 1));
-      }
+      // issued that may still be landing are s_break .. s_break + NST - 1; let
+      // them land, then leave without output
+      if (threadIdx.x == 0)
+         for (int c = s_break; c < s_break + NST && c < nchunks; ++c)
+            async::mbar_wait_quiet(&full[c % NST], (uint32_t)((c / NST) & 1));
       return;
    }
    if (PACKED) {
@@ -716,12 +722,14 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
    }
 }
 
-inline size_t async_smem(int S, int ach, int wlen) { return 2 * sizeof(float2) * (size_t)S * ach * wlen; }
+inline size_t async_smem(int S, int ach, int wlen, int nst = 2) {
+   return (size_t)nst * sizeof(float2) * (size_t)S * ach * wlen;
+}
 
-template <int S, int ACH, bool PACKED, int PPT>
+template <int S, int ACH, bool PACKED, int PPT, int NST = 2>
 cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& cfg, cudaStream_t st) {
    const int wlen = window_len(cfg.scale, 32, 32);
-   const size_t smem = async_smem(S, ACH, wlen);
+   const size_t smem = async_smem(S, ACH, wlen, NST);
    if (smem > kMaxPairsSmem) return cudaErrorInvalidConfiguration;
    // transaction bytes armed on one mbarrier phase stay below 2^20
    if ((size_t)ACH * wlen * sizeof(float2) * S >= (1u << 20)) return cudaErrorInvalidConfiguration;
@@ -736,7 +744,7 @@ cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& 
       if (e != cudaSuccess) return e;
    }
    if (cfg.mid_event && (e = cudaEventRecord(cfg.mid_event, st)) != cudaSuccess) return e;
-   auto kern = bp_linear_async<S, ACH, PACKED, PPT>;
+   auto kern = bp_linear_async<S, ACH, PACKED, PPT, NST>;
    if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
