@@ -208,6 +208,7 @@ struct risa_gb_backprojection {
    DevBuf pairs, err;
    DevBuf rowbase, colbase;  // adjoint: (hi, lo) line starts [Pp][N]
    DevBuf adj;               // adjoint: slice-interleaved image copies (reserve_adjoint)
+   DevBuf tile_win;          // staged variants: window start + origin per tile and angle
    BPCfg cfg(bool fused_mask) const {
       BPCfg c;
       c.Pp = g.Pp; c.Dp = g.Dp; c.N = g.N;
@@ -228,6 +229,7 @@ struct risa_gb_backprojection {
       c.err = err.as<int>();
       c.rowbase = rowbase.as<float2>();
       c.colbase = colbase.as<float2>();
+      c.tile_win = tile_win.as<int2>();
       c.adj_scratch = adj.p;
       c.adj_scratch_bytes = adj.bytes;
       return c;
@@ -745,6 +747,8 @@ risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* gi, const r
    RG_TRY(h->err.alloc(sizeof(int)));
    RG_CUDA(cudaMemset(h->err.p, 0, sizeof(int)));
    if (h->p.interp == RISA_GB_INTERP_LINEAR) {
+      RG_TRY(h->tile_win.upload(bp_tile_windows(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(), t.t0.data(),
+                                                h->g.Pp, h->g.N)));
       RG_TRY(h->rowbase.upload(bp_line_starts(t.t0.data(), t.bd.data(), h->g.Pp, h->g.N)));
       RG_TRY(h->colbase.upload(bp_line_starts(t.t0.data(), t.ad.data(), h->g.Pp, h->g.N)));
    }

@@ -13,6 +13,7 @@
 // ~1e-5 bins even for 1024+ bin detectors.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include <type_traits>
 
@@ -542,14 +543,23 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
       if (lane < na) {
          const int ang = ch * ACH + lane;
          const float a = __ldg(cfg.a + ang), b = __ldg(cfg.b + ang);
-         double base;
-         const int w0 = tile_window_start(cfg, ang, x0, y0, a, b, &base);
+         int w0;
+         float rel;
+         if (cfg.tile_win) {  // the host's table of the same FP64 arithmetic
+            const int2 e = __ldg(cfg.tile_win + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * Pp + ang);
+            w0 = e.x;
+            rel = __int_as_float(e.y);
+         } else {
+            double base;
+            w0 = tile_window_start(cfg, ang, x0, y0, a, b, &base);
+            rel = (float)(base - (double)w0 - 0.5);
+         }
          int u0 = w0 + cfg.win_lo;
          if (u0 < 0 || u0 + wlen > wp) {  // never with host-sized padding
             atomicCAS(cfg.err, 0, 4);
             u0 = min(max(u0, 0), wp - wlen);
          }
-         r.par = make_float4(a, b, (float)(base - (double)w0 - 0.5), 0.f);
+         r.par = make_float4(a, b, rel, 0.f);
          r.u0 = u0;
       }
       return r;
@@ -1010,6 +1020,30 @@ void bp_window_extent(const float* a, const float* b, const double* ad, const do
    // two bins of slack either side; k = u - win_lo
    *win_lo = (int)(2 - lo);
    *win_len = (int)(hi - lo + 4);
+}
+
+std::vector<int2> bp_tile_windows(const float* a, const float* b, const double* ad, const double* bd,
+                                  const double* t0, int Pp, int N) {
+   // tile_window_start of every 32 x 32 tile and angle, in the same rounded
+   // FP64 steps (host code is compiled without floating-point contraction)
+   const int tiles = (N + 31) / 32;
+   std::vector<int2> out((size_t)tiles * tiles * Pp);
+   for (int by = 0; by < tiles; ++by)
+      for (int bx = 0; bx < tiles; ++bx) {
+         const int x0 = bx * 32, y0 = by * 32;
+         int2* row = out.data() + ((size_t)by * tiles + bx) * Pp;
+         for (int i = 0; i < Pp; ++i) {
+            const double base = (t0[i] + (double)x0 * ad[i]) + (double)y0 * bd[i];
+            const float ma = 31.f * a[i], mb = 31.f * b[i];
+            const double tmin = (base + (double)std::fmin(0.f, ma)) + (double)std::fmin(0.f, mb);
+            const int w0 = (int)std::floor(tmin) - 2;
+            const float rel = (float)(base - (double)w0 - 0.5);
+            int bits;
+            std::memcpy(&bits, &rel, sizeof(bits));
+            row[i] = make_int2(w0, bits);
+         }
+      }
+   return out;
 }
 
 std::vector<float2> bp_line_starts(const double* t0, const double* step, int Pp, int N) {
