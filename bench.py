@@ -43,7 +43,7 @@ SMEM_BYTES_PER_UPDATE = 8  # one FP32 (midpoint, difference) pair per pixel x an
 SMEM_BYTES_PER_CLK_SM = 128  # nominal shared-memory bandwidth per SM
 # dram__bytes_read.sum + dram__bytes_write.sum of one 64-slice backprojection launch
 # (profiles/bp_staged_fbp512_ncu.txt)
-BP_DRAM_BYTES_PER_LAUNCH = 729.4e6
+BP_DRAM_BYTES_PER_LAUNCH = 740.4e6
 WORKLOAD_NAME = ("full-rate streaming: 2 planes x 2000 frames of 1000x1152 uint16 fan sinograms, 1% defective "
                  "detectors -> 1024x1024 parallel (pad 2048, Shepp-Logan) -> 512^2 FP32, circular mask")
 

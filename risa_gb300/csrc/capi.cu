@@ -747,8 +747,12 @@ risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* gi, const r
    RG_TRY(h->err.alloc(sizeof(int)));
    RG_CUDA(cudaMemset(h->err.p, 0, sizeof(int)));
    if (h->p.interp == RISA_GB_INTERP_LINEAR) {
-      RG_TRY(h->tile_win.upload(bp_tile_windows(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(), t.t0.data(),
-                                                h->g.Pp, h->g.N)));
+      // 8 B per tile and angle (2 MB for 512^2 x 1024 angles); very large
+      // geometries keep computing the window starts on the device instead
+      const size_t tiles = (size_t)((h->g.N + 31) / 32) * ((h->g.N + 31) / 32);
+      if (tiles * (size_t)h->g.Pp * sizeof(int2) <= ((size_t)256 << 20))
+         RG_TRY(h->tile_win.upload(bp_tile_windows(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(), t.t0.data(),
+                                                   h->g.Pp, h->g.N)));
       RG_TRY(h->rowbase.upload(bp_line_starts(t.t0.data(), t.bd.data(), h->g.Pp, h->g.N)));
       RG_TRY(h->colbase.upload(bp_line_starts(t.t0.data(), t.ad.data(), h->g.Pp, h->g.N)));
    }
