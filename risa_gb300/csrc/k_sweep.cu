@@ -9,6 +9,7 @@
 // the backprojection kernels, fused circular mask.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "async_copy.h"
 #include "fft_r16.cuh"
@@ -175,17 +176,26 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
          if (lane < na) {
             const int ang = ch * kSweepACH + lane;
             const float a = __ldg(I.a + ang), b = __ldg(I.b + ang);
-            const double base = __dadd_rn(__dadd_rn(__ldg(I.t0 + ang), __dmul_rn((double)x0, __ldg(I.ad + ang))),
-                                          __dmul_rn((double)y0, __ldg(I.bd + ang)));
-            const double tmin = __dadd_rn(__dadd_rn(base, (double)fminf(0.f, __fmul_rn(31.f, a))),
-                                          (double)fminf(0.f, __fmul_rn(31.f, b)));
-            const int w0 = ((int)floor(tmin) - 2) & ~1;  // even start: 16-byte aligned copies
+            int w0;
+            float rel;
+            if (I.tile_win) {  // the host's table of the same FP64 arithmetic
+               const int2 e = __ldg(I.tile_win + (size_t)tile * Pp + ang);
+               w0 = e.x;
+               rel = __int_as_float(e.y);
+            } else {
+               const double base = __dadd_rn(__dadd_rn(__ldg(I.t0 + ang), __dmul_rn((double)x0, __ldg(I.ad + ang))),
+                                             __dmul_rn((double)y0, __ldg(I.bd + ang)));
+               const double tmin = __dadd_rn(__dadd_rn(base, (double)fminf(0.f, __fmul_rn(31.f, a))),
+                                             (double)fminf(0.f, __fmul_rn(31.f, b)));
+               w0 = ((int)floor(tmin) - 2) & ~1;  // even start: 16-byte aligned copies
+               rel = (float)(base - (double)w0 - 0.5);
+            }
             int u0 = w0 + I.win_lo;
             if (u0 < 0 || u0 + W > I.win_len) {  // never with host-sized padding
                atomicCAS(A.err, 0, 4);
                u0 = min(max(u0, 0), I.win_len - W) & ~1;
             }
-            S.par[st][lane] = make_float4(a, b, (float)(base - (double)w0 - 0.5), 0.f);
+            S.par[st][lane] = make_float4(a, b, rel, 0.f);
             async::bulk_load(wsm + (size_t)(st * kSweepACH + lane) * W, prow + (size_t)ang * I.win_len + u0,
                              win_bytes, &full[st]);
          }
@@ -347,6 +357,26 @@ void sweep_window_extent(const float* a, const float* b, const double* ad, const
    // two bins of slack either side, both values even
    *win_lo = (int)(2 - lo);
    *win_len = (int)(hi - lo + 4);
+}
+
+void sweep_tile_windows(const float* a, const float* b, const double* ad, const double* bd, const double* t0,
+                        int Pp, int N, std::vector<int2>& out) {
+   // mirrors sweep_tile (host code is compiled without floating-point contraction)
+   const int tiles_x = (N + 31) / 32;
+   out.reserve(out.size() + (size_t)tiles_x * tiles_x * Pp);
+   for (int t = 0; t < tiles_x * tiles_x; ++t) {
+      const int x0 = (t % tiles_x) * 32, y0 = (t / tiles_x) * 32;
+      for (int i = 0; i < Pp; ++i) {
+         const double base = (t0[i] + (double)x0 * ad[i]) + (double)y0 * bd[i];
+         const float ma = 31.f * a[i], mb = 31.f * b[i];
+         const double tmin = (base + (double)std::fmin(0.f, ma)) + (double)std::fmin(0.f, mb);
+         const int w0 = ((int)std::floor(tmin) - 2) & ~1;
+         const float rel = (float)(base - (double)w0 - 0.5);
+         int bits;
+         std::memcpy(&bits, &rel, sizeof(bits));
+         out.push_back(make_int2(w0, bits));
+      }
+   }
 }
 
 size_t sweep_smem_bytes(int max_wlen2) {

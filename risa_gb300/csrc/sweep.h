@@ -16,6 +16,7 @@
 // groups never wait, and every awaited item was taken earlier by a running
 // CTA, so the wait always ends without co-residency of the grid.
 #pragma once
+#include <vector>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -45,6 +46,8 @@ struct SweepInst {
    const double* t0;
    const float2* h;             // [len] frequency response, 1/len included
    const SweepRepair* repair;   // [Dp] or nullptr
+   const int2* tile_win;        // [tile][angle] (even window start, bits of the float origin coordinate),
+                                // sweep_tile_windows; nullptr: computed in FP64 by the tile
 };
 
 enum SweepKind { kSweepRows = 0, kSweepTile = 1 };
@@ -76,6 +79,11 @@ int sweep_window_len(float scale);
 // Padding of an instance's pair sinogram (mirrors the tile kernel's arithmetic).
 void sweep_window_extent(const float* a, const float* b, const double* ad, const double* bd, const double* t0,
                          int Pp, int N, int wlen2, bool masking, int* win_lo, int* win_len);
+// The tile kernel's window start and window-relative origin of every 32 x 32
+// tile and angle of an instance ([tile][angle]), in the same rounded FP64
+// steps, appended to `out`.
+void sweep_tile_windows(const float* a, const float* b, const double* ad, const double* bd, const double* t0,
+                        int Pp, int N, std::vector<int2>& out);
 size_t sweep_smem_bytes(int max_wlen2);
 cudaError_t launch_sweep(const SweepArgs& a, int max_wlen2, cudaStream_t st, int* grid_out);
 

@@ -24,6 +24,7 @@ struct risa_gb_sweep {
    size_t raw_total = 0, img_total = 0, pair_total = 0;
    int max_wlen2 = 0, n_items = 0, grid = 0;
    DevBuf d_inst, d_items, d_f32, d_f64, d_h, d_rep, d_pairs, d_twp[4], d_cnt, d_times;
+   DevBuf d_win;  // per instance [tile][angle] window starts (sweep_tile_windows)
    // d_cnt: [next][err][rows_done n][tiles_done n]; d_times: [t_first n][t_done n][t_launch]
    int* next() const { return d_cnt.as<int>(); }
    int* err() const { return d_cnt.as<int>() + 1; }
@@ -90,7 +91,8 @@ risa_gb_status risa_gb_sweep_create(const risa_gb_sweep_instance* in, int n, ris
    std::vector<double> f64;
    std::vector<float2> hs;
    std::vector<SweepRepair> reps;
-   std::vector<size_t> o_f32(n), o_f64(n), o_h(n), o_rep(n, (size_t)-1);
+   std::vector<size_t> o_f32(n), o_f64(n), o_h(n), o_rep(n, (size_t)-1), o_win(n, (size_t)-1);
+   std::vector<int2> win;
    for (int i = 0; i < n; ++i) {
       const risa_gb_sweep_instance& s = in[i];
       if (s.n_pixels < 16 || s.n_par_proj < 1 || s.n_par_det < 2 || s.n_par_det > 65535 ||
@@ -143,6 +145,12 @@ risa_gb_status risa_gb_sweep_create(const risa_gb_sweep_instance* in, int n, ris
       h->raw_total += (size_t)g.Pp * g.Dp;
       h->img_total += (size_t)g.N * g.N;
       h->pair_total += (size_t)g.Pp * I.win_len;
+      // the tiles' window starts, built here once (8 B per tile and angle, up
+      // to 1 GiB for the whole sweep; later instances compute them in FP64)
+      if ((win.size() + (size_t)I.tiles * g.Pp) * sizeof(int2) <= ((size_t)1 << 30)) {
+         o_win[i] = win.size();
+         sweep_tile_windows(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(), t.t0.data(), g.Pp, g.N, win);
+      }
       o_f32[i] = f32.size();
       f32.insert(f32.end(), t.a.begin(), t.a.end());
       f32.insert(f32.end(), t.b.begin(), t.b.end());
@@ -162,6 +170,7 @@ risa_gb_status risa_gb_sweep_create(const risa_gb_sweep_instance* in, int n, ris
    RG_TRY(h->d_f64.upload(f64));
    RG_TRY(h->d_h.upload(hs));
    RG_TRY(h->d_rep.upload(reps));
+   RG_TRY(h->d_win.upload(win));
    for (int i = 0; i < n; ++i) {
       SweepInst& I = h->inst[i];
       I.a = h->d_f32.as<float>() + o_f32[i];
@@ -171,6 +180,7 @@ risa_gb_status risa_gb_sweep_create(const risa_gb_sweep_instance* in, int n, ris
       I.t0 = I.bd + I.Pp;
       I.h = h->d_h.as<float2>() + o_h[i];
       I.repair = o_rep[i] == (size_t)-1 ? nullptr : h->d_rep.as<SweepRepair>() + o_rep[i];
+      I.tile_win = o_win[i] == (size_t)-1 ? nullptr : h->d_win.as<int2>() + o_win[i];
    }
    RG_TRY(h->d_inst.upload(h->inst));
    // work list: rows(0), rows(1), tiles(0), rows(2), tiles(1), ..., tiles(n-1)
