@@ -928,23 +928,24 @@ __global__ void __launch_bounds__(128) bp_adjoint_rows(const float4* __restrict_
    const float inv = 1.0f / s_hi;  // |s_hi| >= scale / sqrt(2) > 0
    const float4* im = (along_x ? P : PT) + (size_t)g * N * N * 2;
    const float kf = (float)k;
+   // The pixels of a row within one bin of k lie in the open interval from
+   // jlo = (-/+1 - t0) / s of length 2 / |s|; the candidates are the
+   // ncand consecutive integers from ceil(jlo - 1e-3) (1e-3 pixel covers the
+   // FP32 error of jlo, ~1e-4 at these sizes), each then tested exactly.
+   const float lo_num = s_hi > 0.f ? -1.f : 1.f;
+   const int ncand = (int)floorf(2.f * fabsf(inv) + 0.002f) + 1;
    float acc[8];
 #pragma unroll
    for (int s = 0; s < 8; ++s) acc[s] = 0.f;
    for (int r = 0; r < N; ++r) {
       const float2 hb = s_line[r];
       const float t_hi = hb.x - kf, t_lo = hb.y;
-      const float t0 = t_hi + t_lo;
-      float ja = (-1.f - t0) * inv, jb = (1.f - t0) * inv;
-      if (ja > jb) {
-         const float tt = ja;
-         ja = jb;
-         jb = tt;
-      }
-      if (jb < 0.f || ja > (float)(N - 1)) continue;
-      const int js = max(0, (int)floorf(ja)), je = min(N - 1, (int)ceilf(jb));
+      const float jlo = (lo_num - (t_hi + t_lo)) * inv;
+      const int j1 = (int)ceilf(jlo - 1e-3f);
       const float4* row = im + (size_t)r * N * 2;
-      for (int j = js; j <= je; ++j) {
+      for (int c = 0; c < ncand; ++c) {
+         const int j = j1 + c;
+         if ((unsigned)j >= (unsigned)N) continue;
          const float jf = (float)j;
          const float d = fabsf(fmaf(jf, s_hi, t_hi) + fmaf(jf, s_lo, t_lo));
          if (d < 1.f) {
