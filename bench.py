@@ -41,9 +41,10 @@ FRAMES_PER_PLANE = 2000
 FLOPS_PER_UPDATE = 6  # ray coordinate FMA (2) + weight add (1) + interpolation FMA (2) + accumulate (1)
 SMEM_BYTES_PER_UPDATE = 8  # one FP32 (midpoint, difference) pair per pixel x angle and slice
 SMEM_BYTES_PER_CLK_SM = 128  # nominal shared-memory bandwidth per SM
-# dram__bytes_read.sum + dram__bytes_write.sum of one 64-slice backprojection launch
-# (profiles/bp_staged_fbp512_ncu.txt)
-BP_DRAM_BYTES_PER_LAUNCH = 740.4e6
+# dram__bytes_read.sum + dram__bytes_write.sum of a 64-slice backprojection launch
+# (profiles/bp_staged_fbp512_ncu.txt): the pair records read once and the images
+# written, both proportional to the slices, so a launch of B slices moves B/64 of it
+BP_DRAM_BYTES_PER_SLICE = 740.4e6 / 64
 WORKLOAD_NAME = ("full-rate streaming: 2 planes x 2000 frames of 1000x1152 uint16 fan sinograms, 1% defective "
                  "detectors -> 1024x1024 parallel (pad 2048, Shepp-Logan) -> 512^2 FP32, circular mask")
 
@@ -55,7 +56,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--frames", type=int, default=FRAMES_PER_PLANE, help="frames per plane")
-    ap.add_argument("--batch", type=int, default=64, help="frames per engine chunk (multiple of 2)")
+    ap.add_argument("--batch", type=int, default=256, help="frames per engine chunk (multiple of 2)")
     ap.add_argument("--distinct", type=int, default=8, help="distinct synthetic frames per plane")
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/roofline/cpu legs")
     ap.add_argument("--bp-variant", type=int, default=-1,
@@ -191,11 +192,15 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     L = WORKLOAD["n_planes"]
-    B = args.batch - args.batch % L
     g = rg.make_geometry(**WORKLOAD)
     p = rg.make_params(filter_type="sheppLogan", defects=True, masking=True)
     sc = synthetic_scan(args.frames, args.distinct)
     n = sc.raw.shape[0]
+    # a chunk never holds more frames than the job (every enqueue below reads B frames)
+    B = min(args.batch, n)
+    B -= B % L
+    if B < L:
+        raise SystemExit("bench.py: --batch and --frames leave no whole plane group per chunk")
     Pf, Df, N = WORKLOAD["n_fan_proj"], WORKLOAD["n_fan_det"], WORKLOAD["n_pixels"]
     Pp, Dp = WORKLOAD["n_par_proj"], WORKLOAD["n_par_det"]
     fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=B)
@@ -330,7 +335,8 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     out["roofline"] = {
         "kernel": f"bp_linear_async ({rg.Backprojection.variant_name(variant)})", "bound": "smem",
         "achieved": smem_gbs, "peak": smem_peak, "unit": "GB/s", "frac": smem_gbs / smem_peak,
-        "traffic": BP_DRAM_BYTES_PER_LAUNCH,
+        "traffic": BP_DRAM_BYTES_PER_SLICE * B,
+        "traffic_source": "ncu capture of a 64-slice launch, scaled by slices per launch",
         "work": f"{SMEM_BYTES_PER_UPDATE} B of shared-memory reads per pixel x angle update and slice, "
                 f"{inside} in-circle pixels x {Pp} angles x {B} slices per launch",
         "peak_source": f"nominal shared-memory bandwidth {SMEM_BYTES_PER_CLK_SM} B/clk/SM x {sms} SMs x "

@@ -178,6 +178,22 @@ def _check(status: int, what: str):
         raise RisaError(status, what, last_error())
 
 
+def _nbytes(x) -> Optional[int]:
+    """Bytes reachable from the address of a tensor or array (None for raw addresses)."""
+    if hasattr(x, "untyped_storage"):  # torch: from this view's start to its storage's end
+        return x.untyped_storage().nbytes() - x.storage_offset() * x.element_size()
+    if hasattr(x, "nbytes"):
+        return int(x.nbytes)
+    return None
+
+
+def _need(x, nbytes: int, what: str):
+    """Raise before a launch that would read or write past a tensor or array."""
+    have = None if x is None or isinstance(x, int) else _nbytes(x)
+    if have is not None and have < nbytes:
+        raise RisaError(-1, what, f"buffer holds {have} bytes, the call needs {nbytes}")
+
+
 def ptr(x) -> Optional[int]:
     """Device/host address of an int, a torch tensor, a numpy array or None."""
     if x is None:
@@ -545,12 +561,19 @@ class FBP(_Handle):
                "fbp_create")
         self.geom, self.params, self.max_batch = geom, params, max_batch
 
+    def _check_sizes(self, raw, img, n: int, what: str):
+        g = self.geom
+        _need(raw, 2 * n * g.n_fan_proj * g.n_fan_det, what + " (raw frames)")
+        _need(img, 4 * n * g.n_pixels * g.n_pixels, what + " (images)")
+
     def enqueue(self, raw, img, plane: int, batch: int, stream=None):
+        self._check_sizes(raw, img, batch, "fbp_enqueue")
         _check(lib().risa_gb_fbp_enqueue(self._h, ptr(raw), ptr(img), plane, batch, stream_ptr(stream)),
                "fbp_enqueue")
 
     def graph_capture(self, raw, img, plane: int, n_frames: int, stream) -> "Graph":
         """One CUDA graph reconstructing n_frames device frames (chunked by max_batch)."""
+        self._check_sizes(raw, img, n_frames, "fbp_graph_capture")
         gr = Graph()
         _check(lib().risa_gb_fbp_graph_capture(self._h, ptr(raw), ptr(img), plane, n_frames,
                                                stream_ptr(stream), ctypes.byref(gr._h)), "fbp_graph_capture")
@@ -558,6 +581,7 @@ class FBP(_Handle):
         return gr
 
     def run_host(self, host_raw, host_img, n_frames: int, plane: int):
+        self._check_sizes(host_raw, host_img, n_frames, "fbp_run_host")
         _check(lib().risa_gb_fbp_run_host(self._h, ptr(host_raw), ptr(host_img), n_frames, plane),
                "fbp_run_host")
 
@@ -571,6 +595,7 @@ class FBP(_Handle):
         """Mean ms of the engine's stages on one batch (CUDA events on the stream)."""
         import numpy as np
 
+        self._check_sizes(raw, img, batch, "fbp_time_stages")
         ms = np.zeros(6, np.float32)
         _check(lib().risa_gb_fbp_time_stages(self._h, ptr(raw), ptr(img), plane, batch, reps, stream_ptr(stream),
                                              ms.ctypes.data), "fbp_time_stages")

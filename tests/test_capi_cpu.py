@@ -83,3 +83,23 @@ def test_invalid_geometry_rejected_without_gpu():
     p.struct_size = 3
     with pytest.raises(rg.RisaError):
         rg.filter_design_host(rg.make_geometry(), p)
+
+
+def test_fbp_binding_rejects_short_buffers():
+    """The binding checks tensor and array sizes before a launch that would read
+    or write past them (raw frames and images of `batch` frames)."""
+    import types
+
+    import numpy as np
+    import pytest
+
+    import risa_gb300 as rg
+
+    h = types.SimpleNamespace(geom=rg.make_geometry(n_fan_proj=10, n_fan_det=8, n_pixels=4))
+    raw, img = np.zeros((4, 10, 8), np.uint16), np.zeros((4, 4, 4), np.float32)
+    rg.FBP._check_sizes(h, raw, img, 4, "fbp_enqueue")
+    with pytest.raises(rg.RisaError):
+        rg.FBP._check_sizes(h, raw[:3], img, 4, "fbp_enqueue")
+    with pytest.raises(rg.RisaError):
+        rg.FBP._check_sizes(h, raw, img[:2], 4, "fbp_enqueue")
+    rg.FBP._check_sizes(h, 12345, 67890, 4, "fbp_enqueue")  # raw addresses: the caller's responsibility
