@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kThreads) fan2para_gather(const float* __restr
 // Same arithmetic as fan2para_gather, per frame of a quad: each bilinear tap is
 // one 16-byte load covering the quad's 4 frames, the tables are read once per
 // kQuadsPerThread quads of one plane.
-constexpr int kQuadsPerThread = 2;
+constexpr int kQuadsPerThread = 4;
 
 __device__ __forceinline__ float4 bilinear4(const float4* __restrict__ f, uint32_t pk, float u, float v, int Pf,
                                             int Df) {
