@@ -181,10 +181,16 @@ __global__ void __launch_bounds__(kThreads) filter_grad_sum(const float2* __rest
 }
 
 
-// grid.x: groups of 256/(LEN/16) row pairs; dynamic smem: one padded row pair buffer per group.
+// CTAs of max(LEN/16, 128) threads: one row pair per CTA from LEN 2048 up, so a
+// CTA barrier inside the transform waits for 4 warps, not 8.
 template <int LEN>
-__global__ void __launch_bounds__(256, 2) filter_rows_r16(float* __restrict__ sino, int total_rows, FilterCfg cfg) {
-   constexpr int TPF = LEN / 16, FPB = 256 / TPF, PL = LEN + LEN / 16;
+__host__ __device__ constexpr int r16_threads() { return LEN / 16 >= 128 ? LEN / 16 : 128; }
+
+// grid.x: groups of r16_threads/(LEN/16) row pairs; dynamic smem: one padded row pair buffer per group.
+template <int LEN>
+__global__ void __launch_bounds__(r16_threads<LEN>(), 512 / r16_threads<LEN>())
+    filter_rows_r16(float* __restrict__ sino, int total_rows, FilterCfg cfg) {
+   constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF, PL = LEN + LEN / 16;
    using P = R16Plan<LEN>;
    extern __shared__ float2 sm[];
    const int local = threadIdx.x / TPF, lt = threadIdx.x % TPF;
@@ -218,7 +224,7 @@ __global__ void __launch_bounds__(256, 2) filter_rows_r16(float* __restrict__ si
 
 template <int LEN>
 cudaError_t launch_r16(float* sino, int total_rows, const FilterCfg& cfg, cudaStream_t st) {
-   constexpr int TPF = LEN / 16, FPB = 256 / TPF;
+   constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF;
    const size_t smem = sizeof(float2) * (size_t)FPB * (LEN + LEN / 16);
    if (smem > 48 * 1024) {
       cudaError_t e =
@@ -226,7 +232,7 @@ cudaError_t launch_r16(float* sino, int total_rows, const FilterCfg& cfg, cudaSt
       if (e != cudaSuccess) return e;
    }
    const int pairs = (total_rows + 1) / 2;
-   filter_rows_r16<LEN><<<(pairs + FPB - 1) / FPB, 256, smem, st>>>(sino, total_rows, cfg);
+   filter_rows_r16<LEN><<<(pairs + FPB - 1) / FPB, r16_threads<LEN>(), smem, st>>>(sino, total_rows, cfg);
    return cudaGetLastError();
 }
 
@@ -239,9 +245,10 @@ cudaError_t launch_r16(float* sino, int total_rows, const FilterCfg& cfg, cudaSt
 //    mid = (q[k] + q[k+1]) / 2, diff = q[k+1] - q[k], q = 0 outside the detector,
 // for every window bin u -- the filtered sinogram itself is never written.
 template <int LEN>
-__global__ void __launch_bounds__(256, 2) filter_rows_r16_pairs(const float* __restrict__ sino, int batch,
+__global__ void __launch_bounds__(r16_threads<LEN>(), 512 / r16_threads<LEN>())
+    filter_rows_r16_pairs(const float* __restrict__ sino, int batch,
                                                                 FilterCfg cfg, PairsOut po) {
-   constexpr int TPF = LEN / 16, FPB = 256 / TPF, PL = LEN + LEN / 16;
+   constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF, PL = LEN + LEN / 16;
    using P = R16Plan<LEN>;
    extern __shared__ float2 sm[];
    const int local = threadIdx.x / TPF, lt = threadIdx.x % TPF;
@@ -283,7 +290,7 @@ __global__ void __launch_bounds__(256, 2) filter_rows_r16_pairs(const float* __r
 template <int LEN>
 cudaError_t launch_r16_pairs(const float* sino, int batch, const FilterCfg& cfg, const PairsOut& po,
                              cudaStream_t st) {
-   constexpr int TPF = LEN / 16, FPB = 256 / TPF;
+   constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF;
    const size_t smem = sizeof(float2) * (size_t)FPB * (LEN + LEN / 16);
    if (smem > 48 * 1024) {
       cudaError_t e =
@@ -291,7 +298,7 @@ cudaError_t launch_r16_pairs(const float* sino, int batch, const FilterCfg& cfg,
       if (e != cudaSuccess) return e;
    }
    const int pairs = (batch + 1) / 2 * cfg.rows;
-   filter_rows_r16_pairs<LEN><<<(pairs + FPB - 1) / FPB, 256, smem, st>>>(sino, batch, cfg, po);
+   filter_rows_r16_pairs<LEN><<<(pairs + FPB - 1) / FPB, r16_threads<LEN>(), smem, st>>>(sino, batch, cfg, po);
    return cudaGetLastError();
 }
 
