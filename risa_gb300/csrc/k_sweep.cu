@@ -168,13 +168,14 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
       if (warp == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
       const float2* prow = A.pairs + I.pair_off;
       const uint32_t win_bytes = (uint32_t)W * (uint32_t)sizeof(float2);
-      const int nchunks = (Pp + kSweepACH - 1) / kSweepACH;
+      const int ACH = A.ach;
+      const int nchunks = (Pp + ACH - 1) / ACH;
       auto issue = [&](int ch, int st) {
-         const int na = min(kSweepACH, Pp - ch * kSweepACH);
+         const int na = min(ACH, Pp - ch * ACH);
          if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)na * win_bytes);
          __syncwarp();
-         if (lane < na) {
-            const int ang = ch * kSweepACH + lane;
+         for (int l = lane; l < na; l += 32) {  // a lane per angle of the chunk
+            const int ang = ch * ACH + l;
             const float a = __ldg(I.a + ang), b = __ldg(I.b + ang);
             int w0;
             float rel;
@@ -195,8 +196,8 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
                atomicCAS(A.err, 0, 4);
                u0 = min(max(u0, 0), I.win_len - W) & ~1;
             }
-            S.par[st][lane] = make_float4(a, b, rel, 0.f);
-            async::bulk_load(wsm + (size_t)(st * kSweepACH + lane) * W, prow + (size_t)ang * I.win_len + u0,
+            S.par[st][l] = make_float4(a, b, rel, 0.f);
+            async::bulk_load(wsm + (size_t)(st * ACH + l) * W, prow + (size_t)ang * I.win_len + u0,
                              win_bytes, &full[st]);
          }
       };
@@ -232,14 +233,14 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
          const int st = ch & 1;
          if (!async::mbar_wait(&full[st], uses[st] & 1u, A.err, 5)) S.fail = 1;
          ++uses[st];
-         const int na = live ? min(kSweepACH, Pp - ch * kSweepACH) : 0;
+         const int na = live ? min(ACH, Pp - ch * ACH) : 0;
 #pragma unroll 2
          for (int ai = 0; ai < na; ++ai) {
             const float4 q = S.par[st][ai];  // one broadcast load per angle
             const float a = q.x, b = q.y;
             float tm = q.z + (float)xo * a + (float)yo * b;
             const float step = (float)RS * b;
-            const uint32_t abase = wbase + (uint32_t)((st * kSweepACH + ai) * W) * (uint32_t)sizeof(float2);
+            const uint32_t abase = wbase + (uint32_t)((st * ACH + ai) * W) * (uint32_t)sizeof(float2);
 #pragma unroll
             for (int r = 0; r < PPT; ++r) {
                const float v = tm + kSweepMagic;
@@ -379,14 +380,16 @@ void sweep_tile_windows(const float* a, const float* b, const double* ad, const 
    }
 }
 
-size_t sweep_smem_bytes(int max_wlen2) {
+size_t sweep_smem_bytes(int max_wlen2, int ach) {
    const size_t rows = sizeof(float2) * (size_t)4352;  // 4096/LEN row pairs x (LEN + LEN/16), any LEN
-   const size_t tiles = sizeof(float2) * 2 * (size_t)kSweepACH * max_wlen2;
+   const size_t tiles = sizeof(float2) * 2 * (size_t)ach * max_wlen2;
    return std::max(rows, tiles);
 }
 
-cudaError_t launch_sweep(const SweepArgs& a, int max_wlen2, cudaStream_t st, int* grid_out) {
-   const size_t smem = sweep_smem_bytes(max_wlen2);
+cudaError_t launch_sweep(const SweepArgs& args, int max_wlen2, cudaStream_t st, int* grid_out) {
+   SweepArgs a = args;
+   a.ach = sweep_smem_bytes(max_wlen2, kSweepACH) <= 100 * 1024 ? kSweepACH : 32;
+   const size_t smem = sweep_smem_bytes(max_wlen2, a.ach);
    if (smem > 200 * 1024) return cudaErrorInvalidConfiguration;
    cudaError_t e = cudaFuncSetAttribute(sweep_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
    if (e != cudaSuccess) return e;

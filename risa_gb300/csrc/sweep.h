@@ -70,9 +70,12 @@ struct SweepArgs {
    unsigned long long* t_done;    // [instances] end of the last tile, 0 at launch
    unsigned long long* t_launch;  // [1] earliest CTA start, ~0 at launch
    int* err;                      // nonzero: a bounded wait gave up (the CTA stopped)
+   int ach;                       // angles per staged chunk, <= kSweepACH (set by launch_sweep)
 };
 
-constexpr int kSweepACH = 32;  // angles per staged chunk
+// Angles per staged chunk of a tile (one CTA barrier per chunk): 64, or 32
+// where 64 windows of the widest instance do not fit in shared memory.
+constexpr int kSweepACH = 64;
 
 // Staged window length (bins, even) for a given bins-per-pixel scale.
 int sweep_window_len(float scale);
@@ -84,7 +87,7 @@ void sweep_window_extent(const float* a, const float* b, const double* ad, const
 // steps, appended to `out`.
 void sweep_tile_windows(const float* a, const float* b, const double* ad, const double* bd, const double* t0,
                         int Pp, int N, std::vector<int2>& out);
-size_t sweep_smem_bytes(int max_wlen2);
+size_t sweep_smem_bytes(int max_wlen2, int ach = kSweepACH);
 cudaError_t launch_sweep(const SweepArgs& a, int max_wlen2, cudaStream_t st, int* grid_out);
 
 }  // namespace risa_gb
