@@ -159,23 +159,32 @@ __device__ __forceinline__ int r16_time_index(int lt, int b, int r) {
    return lt + b * (LEN / 16) + out_slot<P::R3>(r) * P::NS3;
 }
 
+// Forward FFT of v (first pass's layout) through buf; on return v[b R3 + r]
+// holds the spectrum at index r16_time_index<LEN>(lt, b, r) and buf is free.
+// All threads of the CTA must call it (CTA barriers inside).
+template <int LEN>
+__device__ __forceinline__ void r16_forward(float2 (&v)[16], float2* buf, int lt, const float2* __restrict__ twp) {
+   using P = R16Plan<LEN>;
+   r16_compute<LEN, 16, 1>(lt, v, nullptr);
+   r16_store<LEN, 16, 1>(buf, lt, v);
+   __syncthreads();
+   r16_load<LEN, P::R2>(buf, lt, v);
+   __syncthreads();
+   r16_compute<LEN, P::R2, 16>(lt, v, twp);
+   r16_store<LEN, P::R2, 16>(buf, lt, v);
+   __syncthreads();
+   r16_load<LEN, P::R3>(buf, lt, v);
+   __syncthreads();
+   r16_compute<LEN, P::R3, P::NS3>(lt, v, twp + P::TW3);
+}
+
 template <int LEN>
 __device__ __forceinline__ void r16_filter_core(float2 (&v)[16], float2* buf, int lt, const float2* __restrict__ twp,
                                                 const float2* __restrict__ h, bool adjoint) {
    using P = R16Plan<LEN>;
    const float2* tw2 = twp;
    const float2* tw3 = twp + P::TW3;
-   r16_compute<LEN, 16, 1>(lt, v, nullptr);
-   r16_store<LEN, 16, 1>(buf, lt, v);
-   __syncthreads();
-   r16_load<LEN, P::R2>(buf, lt, v);
-   __syncthreads();
-   r16_compute<LEN, P::R2, 16>(lt, v, tw2);
-   r16_store<LEN, P::R2, 16>(buf, lt, v);
-   __syncthreads();
-   r16_load<LEN, P::R3>(buf, lt, v);
-   __syncthreads();
-   r16_compute<LEN, P::R3, P::NS3>(lt, v, tw3);
+   r16_forward<LEN>(v, buf, lt, twp);
    // Spectrum index of v[b R3 + r] is r16_time_index = lt + (LEN/16) m with
    // m = b + out_slot(r) (16/R3), and LEN = 16 R2 R3 makes m run over 0..15:
    // a thread holds exactly the 16 values the first inverse pass reads

@@ -165,6 +165,92 @@ __global__ void __launch_bounds__(kThreads) filter_grad_partial(const float* __r
    for (int k = threadIdx.x; k < len; k += kThreads) partial[(size_t)blockIdx.x * len + k] = acc[k];
 }
 
+// CTAs of max(LEN/16, 128) threads: one row pair per CTA from LEN 2048 up, so a
+// CTA barrier inside the transform waits for 4 warps, not 8.
+template <int LEN>
+__host__ __device__ constexpr int r16_threads() { return LEN / 16 >= 128 ? LEN / 16 : 128; }
+
+// filter_grad_partial on the radix-16 path (LEN 512..4096): the forward
+// transforms of a row pair of x and of g run in registers (three passes each),
+// the spectra go to shared memory in natural order, and the pair's G conj(X)
+// is added to the CTA's accumulator in the same fixed order as above.
+template <int LEN>
+__global__ void __launch_bounds__(r16_threads<LEN>(), 384 / r16_threads<LEN>())
+    filter_grad_partial_r16(const float* __restrict__ x, const float* __restrict__ g, int total_rows, FilterCfg cfg,
+                            float2* __restrict__ partial, int groups) {
+   constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF, PL = LEN + LEN / 16;
+   using P = R16Plan<LEN>;
+   extern __shared__ float2 sm[];
+   const int local = threadIdx.x / TPF, lt = threadIdx.x % TPF;
+   float2* bx = sm + (size_t)local * 2 * PL;  // X spectrum, padded index
+   float2* bg = bx + PL;                     // transform scratch, then the G spectrum
+   float2* acc = sm + (size_t)FPB * 2 * PL;  // [LEN], shared by the CTA's pairs
+   const int Dp = cfg.Dp;
+   for (int k = threadIdx.x; k < LEN; k += blockDim.x) acc[k] = make_float2(0.f, 0.f);
+   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+      const int pair = grp * FPB + local;
+      const int ra = 2 * pair, rb = 2 * pair + 1;
+      const bool has_a = ra < total_rows, has_b = rb < total_rows;
+      float2 v[16];
+      __syncthreads();  // the previous group's spectra have been read
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+         const int n = lt + r * TPF;
+         v[r] = make_float2((has_a && n < Dp) ? x[(size_t)ra * Dp + n] : 0.f,
+                            (has_b && n < Dp) ? x[(size_t)rb * Dp + n] : 0.f);
+      }
+      r16_forward<LEN>(v, bg, lt, cfg.twp);
+#pragma unroll
+      for (int b = 0; b < 16 / P::R3; ++b)
+#pragma unroll
+         for (int r = 0; r < P::R3; ++r) bx[pad16(r16_time_index<LEN>(lt, b, r))] = v[b * P::R3 + r];
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+         const int n = lt + r * TPF;
+         v[r] = make_float2((has_a && n < Dp) ? g[(size_t)ra * Dp + n] : 0.f,
+                            (has_b && n < Dp) ? g[(size_t)rb * Dp + n] : 0.f);
+      }
+      r16_forward<LEN>(v, bg, lt, cfg.twp);
+#pragma unroll
+      for (int b = 0; b < 16 / P::R3; ++b)
+#pragma unroll
+         for (int r = 0; r < P::R3; ++r) bg[pad16(r16_time_index<LEN>(lt, b, r))] = v[b * P::R3 + r];
+      __syncthreads();
+      for (int p = 0; p < FPB; ++p) {  // pairs of the CTA add in a fixed order
+         if (local == p) {
+            for (int k = lt; k < LEN; k += TPF) {
+               const int nk = (LEN - k) & (LEN - 1);
+               const float2 zk = bx[pad16(k)], zn = bx[pad16(nk)], gk = bg[pad16(k)], gn = bg[pad16(nk)];
+               // X_a = (zk + conj zn)/2, X_b = (zk - conj zn)/(2i); same for G
+               const float2 xa = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+               const float2 xb = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+               const float2 ga = make_float2(0.5f * (gk.x + gn.x), 0.5f * (gk.y - gn.y));
+               const float2 gb = make_float2(0.5f * (gk.y + gn.y), -0.5f * (gk.x - gn.x));
+               // G conj(X)
+               const float2 pa = make_float2(ga.x * xa.x + ga.y * xa.y, ga.y * xa.x - ga.x * xa.y);
+               const float2 pb = make_float2(gb.x * xb.x + gb.y * xb.y, gb.y * xb.x - gb.x * xb.y);
+               acc[k].x += pa.x + pb.x;
+               acc[k].y += pa.y + pb.y;
+            }
+         }
+         __syncthreads();
+      }
+   }
+   for (int k = threadIdx.x; k < LEN; k += blockDim.x) partial[(size_t)blockIdx.x * LEN + k] = acc[k];
+}
+
+template <int LEN>
+cudaError_t launch_grad_partial_r16(const float* x, const float* g, int total_rows, const FilterCfg& cfg,
+                                    float2* partial, int groups, int blocks, cudaStream_t st) {
+   constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF;
+   const size_t smem = sizeof(float2) * ((size_t)FPB * 2 * (LEN + LEN / 16) + LEN);
+   cudaError_t e =
+       cudaFuncSetAttribute(filter_grad_partial_r16<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+   if (e != cudaSuccess) return e;
+   filter_grad_partial_r16<LEN><<<blocks, r16_threads<LEN>(), smem, st>>>(x, g, total_rows, cfg, partial, groups);
+   return cudaGetLastError();
+}
+
 // Sum of the partial spectra in block order, one frequency per thread;
 // spec receives the conjugate (the finish kernel inverts by conj(FFT(conj))).
 __global__ void __launch_bounds__(kThreads) filter_grad_sum(const float2* __restrict__ partial, int blocks, int len,
@@ -180,11 +266,6 @@ __global__ void __launch_bounds__(kThreads) filter_grad_sum(const float2* __rest
    spec[k] = make_float2(sx, -sy);
 }
 
-
-// CTAs of max(LEN/16, 128) threads: one row pair per CTA from LEN 2048 up, so a
-// CTA barrier inside the transform waits for 4 warps, not 8.
-template <int LEN>
-__host__ __device__ constexpr int r16_threads() { return LEN / 16 >= 128 ? LEN / 16 : 128; }
 
 // grid.x: groups of r16_threads/(LEN/16) row pairs; dynamic smem: one padded row pair buffer per group.
 template <int LEN>
@@ -346,13 +427,25 @@ cudaError_t launch_filter_taps_grad(const float* x, const float* g, int batch, c
                                     cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
    const GradPlan gp = grad_plan(cfg, batch);
-   const size_t smem = sizeof(float2) * ((size_t)4 * cfg.len * gp.ppb + cfg.len);
-   if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
-   cudaError_t e = cudaFuncSetAttribute(filter_grad_partial, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem);
+   cudaError_t e = cudaSuccess;
+   // the radix-16 path groups row pairs exactly as the plan does (ppb equal), so
+   // the workspace and the summation order of filter_grad_sum are the same
+   switch (cfg.twp ? cfg.len : 0) {
+      case 512: e = launch_grad_partial_r16<512>(x, g, batch * cfg.rows, cfg, workspace, gp.groups, gp.blocks, st); break;
+      case 1024: e = launch_grad_partial_r16<1024>(x, g, batch * cfg.rows, cfg, workspace, gp.groups, gp.blocks, st); break;
+      case 2048: e = launch_grad_partial_r16<2048>(x, g, batch * cfg.rows, cfg, workspace, gp.groups, gp.blocks, st); break;
+      case 4096: e = launch_grad_partial_r16<4096>(x, g, batch * cfg.rows, cfg, workspace, gp.groups, gp.blocks, st); break;
+      default: {
+         const size_t smem = sizeof(float2) * ((size_t)4 * cfg.len * gp.ppb + cfg.len);
+         if (smem > 227 * 1024) return cudaErrorInvalidConfiguration;
+         e = cudaFuncSetAttribute(filter_grad_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+         if (e != cudaSuccess) return e;
+         filter_grad_partial<<<gp.blocks, kThreads, smem, st>>>(x, g, batch * cfg.rows, cfg, gp.tpp, workspace,
+                                                                gp.groups);
+         e = cudaGetLastError();
+      }
+   }
    if (e != cudaSuccess) return e;
-   filter_grad_partial<<<gp.blocks, kThreads, smem, st>>>(x, g, batch * cfg.rows, cfg, gp.tpp, workspace,
-                                                          gp.groups);
    float2* spec = workspace + (size_t)gp.blocks * cfg.len;
    filter_grad_sum<<<(cfg.len + kThreads - 1) / kThreads, kThreads, 0, st>>>(workspace, gp.blocks, cfg.len, spec);
    const size_t smem2 = sizeof(float2) * 2 * (size_t)cfg.len;

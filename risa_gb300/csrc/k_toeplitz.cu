@@ -499,7 +499,9 @@ EncodeTiled encode_fn() {
    if (!fn) {
       void* p = nullptr;
       cudaDriverEntryPointQueryResult q;
-      if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+      // the driver API's cuTensorMapEncodeTiled as introduced in CUDA 12.0
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+              cudaSuccess &&
           q == cudaDriverEntryPointSuccess)
          fn = reinterpret_cast<EncodeTiled>(p);
    }
