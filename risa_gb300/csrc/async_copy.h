@@ -68,5 +68,16 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
        : "memory");
 }
 
+// 4-, 8- or 16-byte global -> shared copy (cp.async, both addresses aligned to
+// its size). Copies are grouped by cp_async_commit; cp_async_wait_all makes
+// the issuing thread's own copies visible to it.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+   static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
+   asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst)), "l"(src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 }  // namespace async
 }  // namespace risa_gb

@@ -1,0 +1,34 @@
+// Packed two-lane FP32 arithmetic (add/sub/fma.rn.f32x2, sm_100 and later):
+// one instruction performs two operations, each rounded exactly like its
+// scalar .rn counterpart. A pair travels as one 64-bit register pair.
+#pragma once
+#include <cstdint>
+
+namespace risa_gb {
+
+__device__ __forceinline__ unsigned long long f2_pack(float x, float y) {
+   unsigned long long r;
+   asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+   return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float& x, float& y) {
+   asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+   unsigned long long r;
+   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+   return r;
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+   unsigned long long r;
+   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+   return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+   unsigned long long r;
+   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+   return r;
+}
+
+}  // namespace risa_gb

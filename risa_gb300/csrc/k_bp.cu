@@ -18,6 +18,7 @@
 #include <type_traits>
 
 #include "async_copy.h"
+#include "f32x2.cuh"
 #include "kernels.h"
 #include "risa_gb300.h"
 
@@ -426,30 +427,6 @@ __global__ void __launch_bounds__(256) bp_pairs_fill(const float* __restrict__ s
    }
 }
 
-__device__ __forceinline__ unsigned long long f2_pack(float x, float y) {
-   unsigned long long r;
-   asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
-   return r;
-}
-__device__ __forceinline__ void f2_unpack(unsigned long long v, float& x, float& y) {
-   asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
-}
-__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
-   unsigned long long r;
-   asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-   return r;
-}
-__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
-   unsigned long long r;
-   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-   return r;
-}
-__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
-                                                     unsigned long long c) {
-   unsigned long long r;
-   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-   return r;
-}
 __device__ __forceinline__ float4 lds128(uint32_t addr) {
    float4 v;
    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));

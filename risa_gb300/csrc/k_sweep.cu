@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "async_copy.h"
+#include "f32x2.cuh"
 #include "fft_r16.cuh"
 #include "kernels.h"
 #include "sweep.h"
@@ -117,6 +118,10 @@ __device__ void sweep_rows(const SweepArgs& A, const SweepInst& I, int index, fl
 
 struct TileShared {
    float4 par[2][kSweepACH];  // per angle of a chunk: (a, b, window-relative coordinate, unused)
+   // table entries of the next chunk to issue, prefetched by cp.async one
+   // chunk ahead (slot = chunk & 1)
+   float pre_a[2][kSweepACH], pre_b[2][kSweepACH];
+   int2 pre_win[2][kSweepACH];
    int ok, fail;
 };
 
@@ -170,20 +175,47 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
       const uint32_t win_bytes = (uint32_t)W * (uint32_t)sizeof(float2);
       const int ACH = A.ach;
       const int nchunks = (Pp + ACH - 1) / ACH;
-      auto issue = [&](int ch, int st) {
+      // With the host's window table, warp 0 fetches the table entries of
+      // chunk ch + 3 by cp.async while the CTA works on chunk ch + 1, so the
+      // refill after a chunk's barrier reads them from shared memory instead
+      // of waiting on global loads that every other warp would wait for at
+      // the next barrier.
+      const bool pre = I.tile_win != nullptr;
+      auto prefetch = [&](int ch) {
+         const int na = min(ACH, Pp - ch * ACH), s = ch & 1;
+         for (int l = lane; l < na; l += 32) {
+            const int ang = ch * ACH + l;
+            async::cp_async<4>(&S.pre_a[s][l], I.a + ang);
+            async::cp_async<4>(&S.pre_b[s][l], I.b + ang);
+            async::cp_async<8>(&S.pre_win[s][l], I.tile_win + (size_t)tile * Pp + ang);
+         }
+         async::cp_async_commit();
+      };
+      auto issue = [&](int ch, int st, bool from_pre) {
          const int na = min(ACH, Pp - ch * ACH);
+         if (from_pre) async::cp_async_wait_all();
          if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)na * win_bytes);
          __syncwarp();
          for (int l = lane; l < na; l += 32) {  // a lane per angle of the chunk
             const int ang = ch * ACH + l;
-            const float a = __ldg(I.a + ang), b = __ldg(I.b + ang);
+            float a, b, rel;
             int w0;
-            float rel;
-            if (I.tile_win) {  // the host's table of the same FP64 arithmetic
+            if (from_pre) {  // this lane's own prefetched entries
+               const int s = ch & 1;
+               a = S.pre_a[s][l];
+               b = S.pre_b[s][l];
+               const int2 e = S.pre_win[s][l];
+               w0 = e.x;
+               rel = __int_as_float(e.y);
+            } else if (I.tile_win) {  // the host's table of the same FP64 arithmetic
+               a = __ldg(I.a + ang);
+               b = __ldg(I.b + ang);
                const int2 e = __ldg(I.tile_win + (size_t)tile * Pp + ang);
                w0 = e.x;
                rel = __int_as_float(e.y);
             } else {
+               a = __ldg(I.a + ang);
+               b = __ldg(I.b + ang);
                const double base = __dadd_rn(__dadd_rn(__ldg(I.t0 + ang), __dmul_rn((double)x0, __ldg(I.ad + ang))),
                                              __dmul_rn((double)y0, __ldg(I.bd + ang)));
                const double tmin = __dadd_rn(__dadd_rn(base, (double)fminf(0.f, __fmul_rn(31.f, a))),
@@ -202,8 +234,9 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
          }
       };
       if (warp == 0) {
-         issue(0, 0);
-         if (nchunks > 1) issue(1, 1);
+         issue(0, 0, false);
+         if (nchunks > 1) issue(1, 1, false);
+         if (pre && nchunks > 2) prefetch(2);
       }
       __syncthreads();
 
@@ -212,6 +245,7 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
       for (int r = 0; r < PPT; ++r) acc[r] = 0.f;
       const uint32_t wbase = async::smem_u32(wsm);
       const unsigned wmax = (unsigned)(W - 1);
+      const unsigned long long magic2 = f2_pack(kSweepMagic, kSweepMagic);
       bool failed = false;
       // Bit r: the warp's 8 x 4 pixel block of step r lies (partly) in the
       // image and, with the mask, (partly) inside the circle (exact test, as
@@ -238,17 +272,28 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
          for (int ai = 0; ai < na; ++ai) {
             const float4 q = S.par[st][ai];  // one broadcast load per angle
             const float a = q.x, b = q.y;
-            float tm = q.z + (float)xo * a + (float)yo * b;
+            const float tm = q.z + (float)xo * a + (float)yo * b;
             const float step = (float)RS * b;
             const uint32_t abase = wbase + (uint32_t)((st * ACH + ai) * W) * (uint32_t)sizeof(float2);
+            // pixel steps (r, r + 1) as one f32x2 pair: the ray coordinate,
+            // its rounding and the fraction take one instruction per pair
+            unsigned long long t2 = f2_pack(tm, tm + step);
+            const float step2 = 2.f * step;
+            const unsigned long long dt2 = f2_pack(step2, step2);
 #pragma unroll
-            for (int r = 0; r < PPT; ++r) {
-               const float v = tm + kSweepMagic;
-               const float f = tm - (v - kSweepMagic);
-               const unsigned k = min((unsigned)(__float_as_int(v) - kSweepMagicBits), wmax);
-               const float2 p = lds64(abase + k * (uint32_t)sizeof(float2));
-               acc[r] = fmaf(f, p.y, acc[r] + p.x);
-               tm += step;
+            for (int r = 0; r < PPT; r += 2) {
+               const unsigned long long v2 = f2_add(t2, magic2);
+               const unsigned long long fr2 = f2_sub(t2, f2_sub(v2, magic2));
+               float v0, v1, f0, f1;
+               f2_unpack(v2, v0, v1);
+               f2_unpack(fr2, f0, f1);
+               const unsigned k0 = min((unsigned)(__float_as_int(v0) - kSweepMagicBits), wmax);
+               const unsigned k1 = min((unsigned)(__float_as_int(v1) - kSweepMagicBits), wmax);
+               const float2 p0 = lds64(abase + k0 * (uint32_t)sizeof(float2));
+               const float2 p1 = lds64(abase + k1 * (uint32_t)sizeof(float2));
+               acc[r] = fmaf(f0, p0.y, acc[r] + p0.x);
+               acc[r + 1] = fmaf(f1, p1.y, acc[r + 1] + p1.x);
+               t2 = f2_add(t2, dt2);
             }
          }
          __syncthreads();
@@ -256,10 +301,14 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
             if (threadIdx.x == 0) {  // the copies of the next chunk may still be in flight
                if (ch + 1 < nchunks) async::mbar_wait_quiet(&full[st ^ 1], uses[st ^ 1] & 1u);
             }
+            if (warp == 0) async::cp_async_wait_all();  // and a prefetch of table entries
             failed = true;
             break;
          }
-         if (warp == 0 && ch + 2 < nchunks) issue(ch + 2, st);
+         if (warp == 0 && ch + 2 < nchunks) {
+            issue(ch + 2, st, pre);
+            if (pre && ch + 3 < nchunks) prefetch(ch + 3);
+         }
       }
       if (failed) return false;
 #pragma unroll

@@ -266,6 +266,26 @@ def test_fbp_chain_vs_oracle(quirk, defects):
         assert mr < MAX_REL and l2 < MAX_REL, (b, mr, l2)
 
 
+@pytest.mark.parametrize("Pp,Dp", [(93, 96), (96, 90)])
+def test_fbp_rebinning_tiles(Pp, Dp):
+    """The engine's rebinning from frame quads on shapes that end in partial
+    blocks: an odd angle count (93) and a ray count that is not a multiple of
+    32 (90)."""
+    d, sc, g, p, op = _fbp_case(rg.QUIRKS_NONE, False, masking=True, L=2, frames=3)
+    d.update(n_par_proj=Pp, n_par_det=Dp)
+    g = geom(d)
+    n = sc.raw.shape[0]
+    fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=n)
+    img = torch.empty((n, d["n_pixels"], d["n_pixels"]), dtype=torch.float32, device="cuda")
+    fbp.enqueue(dev(sc.raw.view(np.int16)), img, rg.PLANES_INTERLEAVED, n)
+    got = host(img)
+    oref, odark = oracle.attenuation_init(sc.ref, sc.dark, 2, 0.67, 1.5, True, rg.QUIRKS_NONE)
+    exp = oracle.fbp(ns(d), op, oracle.f2p_records(ns(d), rg.QUIRKS_NONE), oref, odark, sc.raw, sc.planes)
+    for b in range(n):
+        mr, l2 = rel_err(got[b], exp[b])
+        assert mr < MAX_REL and l2 < MAX_REL, (Pp, Dp, b, mr, l2)
+
+
 def test_fbp_fused_filter_staging():
     """Staged backprojection variants with a radix-16 filter length: the filter
     writes the pair records itself (no staging pass); an odd batch leaves the
