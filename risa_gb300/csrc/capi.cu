@@ -154,15 +154,38 @@ struct risa_gb_fan2para {
    DevBuf adj_rowptr, adj_col, adj_w;
    int adj_nnz_stride = 0;
    bool adj_ready = false;
+   DevBuf srel, boxes;  // staged gather from frame quads (build_f2p_staged), engine only
+   int stage_entries = 0;
    F2PCfg cfg(int plane) const {
       F2PCfg c;
       c.Pf = g.Pf; c.Df = g.Df; c.Pp = g.Pp; c.Dp = g.Dp; c.L = g.L; c.plane = plane;
       c.packed = packed.as<uint32_t>();
       c.u = u.as<float>();
       c.v = v.as<float>();
+      if (stage_entries > 0) {
+         c.srel = srel.as<uint32_t>();
+         c.boxes = boxes.as<int4>();
+         c.stage_entries = stage_entries;
+      }
       return c;
    }
 };
+
+// The engine's rebinning from frame quads stages each output tile's fan boxes
+// in shared memory; without boxes that fit, it gathers from global memory.
+static risa_gb_status prepare_f2p_staged(risa_gb_fan2para* h) {
+   std::vector<F2PGather> planes;
+   RG_TRY(build_f2p_gather_all(h->g, h->p, &planes));
+   std::vector<uint32_t> pk;
+   for (auto& t : planes) pk.insert(pk.end(), t.packed.begin(), t.packed.end());
+   F2PStaged st;
+   build_f2p_staged(pk.data(), h->g.L, h->g.Pf, h->g.Df, h->g.Pp, h->g.Dp, &st);
+   if (st.stage_entries <= 0) return RISA_GB_OK;
+   RG_TRY(h->srel.upload(st.rel));
+   RG_TRY(h->boxes.upload(st.boxes));
+   h->stage_entries = st.stage_entries;
+   return RISA_GB_OK;
+}
 
 struct risa_gb_filter {
    Geometry g;
@@ -963,6 +986,7 @@ risa_gb_status risa_gb_fbp_create(const risa_gb_geometry* gi, const risa_gb_para
    if (h->p.defects) RG_TRY(risa_gb_defects_create(gi, pi, max_batch, &h->defects));
    RG_TRY(risa_gb_attenuation_create(gi, pi, ref_frames, n_ref, dark_frames, n_dark, &h->atten));
    RG_TRY(risa_gb_fan2para_create(gi, pi, &h->f2p));
+   RG_TRY(prepare_f2p_staged(h->f2p));
    RG_TRY(risa_gb_filter_create(gi, pi, &h->filt));
    RG_TRY(risa_gb_backprojection_create(gi, pi, &h->bp));
    RG_TRY(risa_gb_masking_create(gi, pi, &h->mask));

@@ -9,6 +9,9 @@
 // from compact per-output tables (index pair + two FP32 weights per ray,
 // built in FP64 on the host). The table entries are loaded once and reused
 // for kFramesPerThread frames of the same plane.
+#include <algorithm>
+#include <vector>
+
 #include "kernels.h"
 
 namespace risa_gb {
@@ -156,6 +159,160 @@ __global__ void __launch_bounds__(kThreads) fan2para_gather_quads(const float4* 
    }
 }
 
+// ---- staged from frame quads ---------------------------------------------------
+// The gather above is bound by L1 wavefronts: a 128-bit load is served in
+// 8-lane phases, and the 8 consecutive rays of a phase straddle two fan
+// projection rows (lines 18 KB apart) almost always, so a tap load costs ~7.5
+// wavefronts instead of 4. Here a CTA owns one tile of 8 angles x 32 rays of
+// one plane and stages, per frame quad, the tile's four fan boxes (one per
+// slot, ~10 x 11 samples each) in shared memory with cp.async -- the box rows
+// sit f2p_box_pitch apart, so the taps of rows r and r + 1 in one phase hit
+// different banks -- and gathers the taps from there: 4 wavefronts per tap
+// load plus ~1 per 9.5 taps for the staging. Same arithmetic as
+// fan2para_gather_quads, so the same bits.
+constexpr int kStageThreads = kF2PTileAngles * kF2PTileRays;  // one output per thread
+constexpr int kStageSlotsPerThread = kF2PMaxStageEntries / kStageThreads;
+constexpr int kStageQuadsPerCTA = 8;
+static_assert(kStageThreads == 256, "one warp per tile angle");
+
+__device__ __forceinline__ float4 lds128_f4(uint32_t addr) {
+   float4 v;
+   asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+   return v;
+}
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__device__ __forceinline__ float4 bilinear4_smem(uint32_t a, uint32_t pitch_bytes, float u, float v) {
+   const float4 w1 = lds128_f4(a), w2 = lds128_f4(a + 16u);
+   const float4 w3 = lds128_f4(a + pitch_bytes), w4 = lds128_f4(a + pitch_bytes + 16u);
+   float4 r;
+   {
+      const float v1 = w1.x + u * (w3.x - w1.x), v2 = w2.x + u * (w4.x - w2.x);
+      r.x = v1 + v * (v2 - v1);
+   }
+   {
+      const float v1 = w1.y + u * (w3.y - w1.y), v2 = w2.y + u * (w4.y - w2.y);
+      r.y = v1 + v * (v2 - v1);
+   }
+   {
+      const float v1 = w1.z + u * (w3.z - w1.z), v2 = w2.z + u * (w4.z - w2.z);
+      r.z = v1 + v * (v2 - v1);
+   }
+   {
+      const float v1 = w1.w + u * (w3.w - w1.w), v2 = w2.w + u * (w4.w - w2.w);
+      r.w = v1 + v * (v2 - v1);
+   }
+   return r;
+}
+
+// grid.x: tiles (angle-tile major), grid.y: (plane, group of kStageQuadsPerCTA quads).
+__global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* __restrict__ fanq,
+                                                                 float* __restrict__ par, F2PCfg cfg, QuadMap qm,
+                                                                 int groups) {
+   extern __shared__ float4 stg[];  // two stages of cfg.stage_entries entries
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int tiles_s = (cfg.Dp + kF2PTileRays - 1) / kF2PTileRays;
+   const int tiles = ((cfg.Pp + kF2PTileAngles - 1) / kF2PTileAngles) * tiles_s;
+   const int tile = blockIdx.x;
+   const int th = (tile / tiles_s) * kF2PTileAngles + warp, sr = (tile % tiles_s) * kF2PTileRays + lane;
+   const bool act = th < cfg.Pp && sr < cfg.Dp;
+   const int no = cfg.Pp * cfg.Dp, o = th * cfg.Dp + sr;
+   const int k = blockIdx.y / groups, g = blockIdx.y % groups;
+   const int plane = qm.plane >= 0 ? qm.plane : k;
+   const int first = g * kStageQuadsPerCTA;
+   const int nq = min(kStageQuadsPerCTA, qm.per_plane - first);
+
+   // this thread's share of the staging, the same for every quad: entry
+   // tid + 256 i of the tile's boxes <- fan sample goff[i] (-1: row padding)
+   const int4* bx = cfg.boxes + ((size_t)plane * tiles + tile) * 4;
+   int4 b[4];
+   int base[5];
+   base[0] = 0;
+#pragma unroll
+   for (int s = 0; s < 4; ++s) {
+      b[s] = __ldg(bx + s);
+      base[s + 1] = base[s] + b[s].z * f2p_box_pitch(b[s].w);
+   }
+   int goff[kStageSlotsPerThread];
+#pragma unroll
+   for (int i = 0; i < kStageSlotsPerThread; ++i) {
+      const int e = threadIdx.x + i * kStageThreads;
+      goff[i] = -1;
+      if (e < base[4]) {
+         // selects, not indexing: the box arrays stay in registers
+         const int4 bb = e < base[1] ? b[0] : e < base[2] ? b[1] : e < base[3] ? b[2] : b[3];
+         const int b0 = e < base[1] ? 0 : e < base[2] ? base[1] : e < base[3] ? base[2] : base[3];
+         const int pitch = f2p_box_pitch(bb.w);
+         const int local = e - b0, row = local / pitch, col = local - row * pitch;
+         if (col < bb.w) {
+            int r = bb.x + row, c = bb.y + col;
+            if (r >= cfg.Pf) r -= cfg.Pf;
+            if (c >= cfg.Df) c -= cfg.Df;
+            goff[i] = r * cfg.Df + c;
+         }
+      }
+   }
+   const size_t fs = (size_t)cfg.Pf * cfg.Df;
+   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(stg);
+   const uint32_t stage_bytes = (uint32_t)cfg.stage_entries * 16u;
+   auto stage = [&](int t) {
+      const float4* src = fanq + (size_t)(k * qm.per_plane + first + t) * fs;
+      const uint32_t dst = sbase + (uint32_t)(t & 1) * stage_bytes + threadIdx.x * 16u;
+#pragma unroll
+      for (int i = 0; i < kStageSlotsPerThread; ++i)
+         if (goff[i] >= 0) cp_async16(dst + (uint32_t)i * (kStageThreads * 16u), src + goff[i]);
+      cp_async_commit();
+   };
+   if (nq > 0) stage(0);
+
+   uint32_t rel[4];
+   float u[4], v[4];
+   const size_t tbase = (size_t)plane * 4 * no + o;
+#pragma unroll
+   for (int s = 0; s < 4; ++s) {
+      rel[s] = act ? __ldg(cfg.srel + tbase + (size_t)s * no) : 0u;
+      u[s] = act ? __ldg(cfg.u + tbase + (size_t)s * no) : 0.f;
+      v[s] = act ? __ldg(cfg.v + tbase + (size_t)s * no) : 0.f;
+   }
+   const int na = (int)(rel[0] >> 31) + (int)(rel[1] >> 31);
+   const int nb = (int)(rel[2] >> 31) + (int)(rel[3] >> 31);
+
+   for (int t = 0; t < nq; ++t) {
+      if (t + 1 < nq) {
+         stage(t + 1);
+         cp_async_wait<1>();
+      } else {
+         cp_async_wait<0>();
+      }
+      __syncthreads();  // every thread's copies of quad t have landed
+      if (act) {
+         const uint32_t sb = sbase + (uint32_t)(t & 1) * stage_bytes;
+         float4 w[4];
+#pragma unroll
+         for (int s = 0; s < 4; ++s)
+            w[s] = (rel[s] >> 31) ? bilinear4_smem(sb + (rel[s] & 0xFFFFu) * 16u, ((rel[s] >> 20) & 0xFFu) * 16u,
+                                                   u[s], v[s])
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+         const float r[4] = {fold(w[0].x, w[1].x, w[2].x, w[3].x, na, nb), fold(w[0].y, w[1].y, w[2].y, w[3].y, na, nb),
+                             fold(w[0].z, w[1].z, w[2].z, w[3].z, na, nb), fold(w[0].w, w[1].w, w[2].w, w[3].w, na, nb)};
+         const int q = k * qm.per_plane + first + t;
+#pragma unroll
+         for (int j = 0; j < 4; ++j) {
+            const int bf = quad_frame(qm, q, j);
+            if (bf >= 0) par[(size_t)bf * no + o] = r[j];
+         }
+      }
+      __syncthreads();  // stage t & 1 is refilled with quad t + 2 next
+   }
+}
+
 // Transpose: fan[t] = sum over parallel samples p of w(p,t) * par[p], from a
 // CSR table grouped by fan sample (one thread per fan sample, no atomics).
 __global__ void __launch_bounds__(kThreads) fan2para_adjoint(const float* __restrict__ par,
@@ -175,6 +332,80 @@ __global__ void __launch_bounds__(kThreads) fan2para_adjoint(const float* __rest
    fan[(size_t)f * nf + t] = acc;
 }
 }  // namespace
+
+void build_f2p_staged(const uint32_t* packed, int L, int Pf, int Df, int Pp, int Dp, F2PStaged* out) {
+   out->boxes.clear();
+   out->rel.clear();
+   out->stage_entries = 0;
+   const int tiles_s = (Dp + kF2PTileRays - 1) / kF2PTileRays;
+   const int tiles_t = (Pp + kF2PTileAngles - 1) / kF2PTileAngles;
+   const int tiles = tiles_t * tiles_s;
+   const size_t no = (size_t)Pp * Dp;
+   std::vector<int4> boxes((size_t)L * tiles * 4);
+   std::vector<uint32_t> rel((size_t)L * 4 * no, 0u);
+   // the shortest circular arc of [0, n) holding every value in xs (sorted
+   // in place): start and length. A full circle gets one more entry (the
+   // start again), so the +1 tap of its last row or column stays in the box.
+   auto arc = [](std::vector<int>& xs, int n, int* start, int* len) {
+      std::sort(xs.begin(), xs.end());
+      xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
+      const int m = (int)xs.size();
+      int gap = -1, at = 0;
+      for (int i = 0; i < m; ++i) {
+         const int d = (i + 1 < m ? xs[i + 1] : xs[0] + n) - xs[i];
+         if (d > gap) gap = d, at = i;
+      }
+      *start = xs[(at + 1) % m];
+      *len = m == n ? n + 1 : n - gap + 1;
+   };
+   int most = 0;
+   std::vector<int> rows, cols;
+   for (int k = 0; k < L; ++k)
+      for (int bt = 0; bt < tiles_t; ++bt)
+         for (int bs = 0; bs < tiles_s; ++bs) {
+            const int tile = bt * tiles_s + bs;
+            int base = 0;
+            for (int s = 0; s < 4; ++s) {
+               const uint32_t* pk = packed + ((size_t)k * 4 + s) * no;
+               rows.clear();
+               cols.clear();
+               for (int i = bt * kF2PTileAngles; i < std::min(Pp, (bt + 1) * kF2PTileAngles); ++i)
+                  for (int j = bs * kF2PTileRays; j < std::min(Dp, (bs + 1) * kF2PTileRays); ++j) {
+                     const uint32_t p = pk[(size_t)i * Dp + j];
+                     if (!(p >> 31)) continue;
+                     const int tb = (int)((p >> 16) & 0x7FFFu), gb = (int)(p & 0xFFFFu);
+                     rows.push_back(tb);
+                     rows.push_back(tb + 1 == Pf ? 0 : tb + 1);
+                     cols.push_back(gb);
+                     cols.push_back(gb + 1 == Df ? 0 : gb + 1);
+                  }
+               int4 bx = make_int4(0, 0, 0, 0);
+               if (!rows.empty()) {
+                  arc(rows, Pf, &bx.x, &bx.z);
+                  arc(cols, Df, &bx.y, &bx.w);
+               }
+               boxes[((size_t)k * tiles + tile) * 4 + s] = bx;
+               const int pitch = f2p_box_pitch(bx.w);
+               if (pitch > 255) return;  // beyond the packed pitch: not staged
+               for (int i = bt * kF2PTileAngles; i < std::min(Pp, (bt + 1) * kF2PTileAngles); ++i)
+                  for (int j = bs * kF2PTileRays; j < std::min(Dp, (bs + 1) * kF2PTileRays); ++j) {
+                     const size_t o = (size_t)i * Dp + j;
+                     const uint32_t p = pk[o];
+                     if (!(p >> 31)) continue;
+                     const int tb = (int)((p >> 16) & 0x7FFFu), gb = (int)(p & 0xFFFFu);
+                     const int row = (tb - bx.x + Pf) % Pf, col = (gb - bx.y + Df) % Df;
+                     rel[((size_t)k * 4 + s) * no + o] =
+                         0x80000000u | ((uint32_t)pitch << 20) | (uint32_t)(base + row * pitch + col);
+                  }
+               base += bx.z * pitch;
+            }
+            most = std::max(most, base);
+            if (most > kF2PMaxStageEntries) return;  // not staged
+         }
+   out->boxes = std::move(boxes);
+   out->rel = std::move(rel);
+   out->stage_entries = most;
+}
 
 cudaError_t launch_fan2para(const float* fan, float* par, int batch, const F2PCfg& cfg,
                             cudaStream_t st) {
@@ -196,6 +427,14 @@ cudaError_t launch_fan2para_quads(const float* fanq, float* par, int batch, cons
                                   cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
    const QuadMap qm = make_quad_map(cfg.L, cfg.plane, batch);
+   if (cfg.srel && cfg.boxes && cfg.stage_entries > 0 && cfg.stage_entries <= kF2PMaxStageEntries) {
+      const int groups = (qm.per_plane + kStageQuadsPerCTA - 1) / kStageQuadsPerCTA;
+      const int tiles = ((cfg.Pp + kF2PTileAngles - 1) / kF2PTileAngles) * ((cfg.Dp + kF2PTileRays - 1) / kF2PTileRays);
+      const size_t smem = 2 * (size_t)cfg.stage_entries * sizeof(float4);
+      dim3 grid(tiles, qm.L * groups);
+      fan2para_staged<<<grid, kStageThreads, smem, st>>>(reinterpret_cast<const float4*>(fanq), par, cfg, qm, groups);
+      return cudaGetLastError();
+   }
    const int groups = (qm.per_plane + kQuadsPerThread - 1) / kQuadsPerThread;
    const int no = cfg.Pp * cfg.Dp;
    dim3 grid((no + kThreads - 1) / kThreads, qm.L * groups);

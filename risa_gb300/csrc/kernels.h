@@ -156,7 +156,36 @@ struct F2PCfg {
    const uint32_t* packed;  // [L][4][Pp*Dp]
    const float* u;          // [L][4][Pp*Dp]
    const float* v;          // [L][4][Pp*Dp]
+   // Shared-memory staged gather from frame quads (build_f2p_staged); used by
+   // launch_fan2para_quads when srel is set.
+   const uint32_t* srel = nullptr;  // [L][4][Pp*Dp]
+   const int4* boxes = nullptr;     // [L][tiles][4]
+   int stage_entries = 0;
 };
+// Staged rebinning: the outputs are cut into tiles of kF2PTileAngles angles x
+// kF2PTileRays rays; for every (plane, tile, slot) the fan rows and detector
+// columns its valid outputs' four bilinear taps touch form a box (r0, c0, nr,
+// nc), circular in both directions. A tile's four boxes are staged one after
+// the other in shared memory, rows `f2p_box_pitch(nc)` entries apart (16 bytes
+// per entry: one fan sample of a frame quad), and srel holds, per output and
+// slot: bit 31 valid, bits 20..27 the pitch, bits 0..15 the entry of its
+// first tap in the tile's staged boxes.
+constexpr int kF2PTileAngles = 8, kF2PTileRays = 32;
+constexpr int kF2PMaxStageEntries = 1024;
+__host__ __device__ inline int f2p_box_pitch(int nc) {
+   // the smallest p >= nc with p = 4 (mod 8): rows r and r + 1 of a box fall
+   // half a bank row apart, so a load phase spanning them is conflict-free
+   return nc <= 0 ? 0 : nc + ((12 - (nc & 7)) & 7);
+}
+struct F2PStaged {
+   std::vector<int4> boxes;    // [L][tiles][4]: (r0, c0, nr, nc)
+   std::vector<uint32_t> rel;  // [L][4][Pp*Dp]
+   int stage_entries = 0;      // most entries of one tile's four boxes (0: not staged)
+};
+// From the gather tables ([L][4][Pp*Dp], bit 31 valid, bits 16..30 fan row,
+// bits 0..15 fan column). Leaves `out` empty when a tile's boxes exceed
+// kF2PMaxStageEntries.
+void build_f2p_staged(const uint32_t* packed, int L, int Pf, int Df, int Pp, int Dp, F2PStaged* out);
 cudaError_t launch_fan2para(const float* fan, float* par, int batch, const F2PCfg& cfg,
                             cudaStream_t st);
 // Rebinning from frame quads (see QuadMap) into per-frame parallel sinograms.

@@ -286,6 +286,31 @@ def test_fbp_rebinning_tiles(Pp, Dp):
         assert mr < MAX_REL and l2 < MAX_REL, (Pp, Dp, b, mr, l2)
 
 
+def test_fbp_staged_rebinning():
+    """A parallel sampling fine enough for the engine to stage each output
+    tile's fan boxes in shared memory (404 angles x 344 rays from 500 x 432:
+    partial angle and ray tiles), two planes, interleaved and fixed-plane
+    batches, 3 frames per plane (a partly filled frame quad)."""
+    d, sc, g, p, op = _fbp_case(rg.QUIRKS_NONE, True, masking=True, L=2, frames=3)
+    d.update(n_par_proj=404, n_par_det=344, n_pixels=128)
+    g = geom(d)
+    n = sc.raw.shape[0]
+    oref, odark = oracle.attenuation_init(sc.ref, sc.dark, 2, 0.67, 1.5, True, rg.QUIRKS_NONE)
+    rec = oracle.f2p_records(ns(d), rg.QUIRKS_NONE)
+    fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=n)
+    raw = sc.raw.view(np.int16)
+    N = d["n_pixels"]
+    plane1 = np.flatnonzero(sc.planes == 1)
+    for plane, idx in ((rg.PLANES_INTERLEAVED, np.arange(n)), (1, plane1)):
+        exp = oracle.fbp(ns(d), op, rec, oref, odark, sc.raw[idx], sc.planes[idx])
+        img = torch.empty((len(idx), N, N), dtype=torch.float32, device="cuda")
+        fbp.enqueue(dev(raw[idx]), img, plane, len(idx))
+        got = host(img)
+        for b in range(len(idx)):
+            mr, l2 = rel_err(got[b], exp[b])
+            assert mr < MAX_REL and l2 < MAX_REL, (plane, b, mr, l2)
+
+
 def test_fbp_fused_filter_staging():
     """Staged backprojection variants with a radix-16 filter length: the filter
     writes the pair records itself (no staging pass); an odd batch leaves the
