@@ -24,6 +24,11 @@ __device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsig
    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
    return r;
 }
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+   unsigned long long r;
+   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+   return r;
+}
 __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
                                                      unsigned long long c) {
    unsigned long long r;

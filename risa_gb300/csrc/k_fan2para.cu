@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "f32x2.cuh"
 #include "kernels.h"
 
 namespace risa_gb {
@@ -175,11 +176,6 @@ constexpr int kStageSlotsPerThread = kF2PMaxStageEntries / kStageThreads;
 constexpr int kStageQuadsPerCTA = 8;
 static_assert(kStageThreads == 256, "one warp per tile angle");
 
-__device__ __forceinline__ float4 lds128_f4(uint32_t addr) {
-   float4 v;
-   asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
-   return v;
-}
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
@@ -189,26 +185,25 @@ __device__ __forceinline__ void cp_async_wait() {
    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-__device__ __forceinline__ float4 bilinear4_smem(uint32_t a, uint32_t pitch_bytes, float u, float v) {
-   const float4 w1 = lds128_f4(a), w2 = lds128_f4(a + 16u);
-   const float4 w3 = lds128_f4(a + pitch_bytes), w4 = lds128_f4(a + pitch_bytes + 16u);
-   float4 r;
-   {
-      const float v1 = w1.x + u * (w3.x - w1.x), v2 = w2.x + u * (w4.x - w2.x);
-      r.x = v1 + v * (v2 - v1);
-   }
-   {
-      const float v1 = w1.y + u * (w3.y - w1.y), v2 = w2.y + u * (w4.y - w2.y);
-      r.y = v1 + v * (v2 - v1);
-   }
-   {
-      const float v1 = w1.z + u * (w3.z - w1.z), v2 = w2.z + u * (w4.z - w2.z);
-      r.z = v1 + v * (v2 - v1);
-   }
-   {
-      const float v1 = w1.w + u * (w3.w - w1.w), v2 = w2.w + u * (w4.w - w2.w);
-      r.w = v1 + v * (v2 - v1);
-   }
+__device__ __forceinline__ ulonglong2 lds128_pairs(uint32_t addr) {
+   ulonglong2 v;
+   asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "r"(addr));
+   return v;
+}
+// a + t (b - a) on two frames at once, the contracted form of the scalar lerp
+__device__ __forceinline__ unsigned long long lerp2(unsigned long long a, unsigned long long b,
+                                                    unsigned long long t) {
+   return f2_fma(t, f2_sub(b, a), a);
+}
+// The bilinear tap blend of the gather kernels on the 4 frames of a quad, as
+// two f32x2 pairs (frames 0,1 and 2,3); u2, v2 hold the weight twice.
+__device__ __forceinline__ ulonglong2 bilinear4_smem(uint32_t a, uint32_t pitch_bytes, unsigned long long u2,
+                                                     unsigned long long v2) {
+   const ulonglong2 w1 = lds128_pairs(a), w2 = lds128_pairs(a + 16u);
+   const ulonglong2 w3 = lds128_pairs(a + pitch_bytes), w4 = lds128_pairs(a + pitch_bytes + 16u);
+   ulonglong2 r;
+   r.x = lerp2(lerp2(w1.x, w3.x, u2), lerp2(w2.x, w4.x, u2), v2);
+   r.y = lerp2(lerp2(w1.y, w3.y, u2), lerp2(w2.y, w4.y, u2), v2);
    return r;
 }
 
@@ -273,16 +268,24 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
    if (nq > 0) stage(0);
 
    uint32_t rel[4];
-   float u[4], v[4];
+   unsigned long long u2[4], v2[4];
    const size_t tbase = (size_t)plane * 4 * no + o;
 #pragma unroll
    for (int s = 0; s < 4; ++s) {
       rel[s] = act ? __ldg(cfg.srel + tbase + (size_t)s * no) : 0u;
-      u[s] = act ? __ldg(cfg.u + tbase + (size_t)s * no) : 0.f;
-      v[s] = act ? __ldg(cfg.v + tbase + (size_t)s * no) : 0.f;
+      const float u = act ? __ldg(cfg.u + tbase + (size_t)s * no) : 0.f;
+      const float v = act ? __ldg(cfg.v + tbase + (size_t)s * no) : 0.f;
+      u2[s] = f2_pack(u, u);
+      v2[s] = f2_pack(v, v);
    }
-   const int na = (int)(rel[0] >> 31) + (int)(rel[1] >> 31);
-   const int nb = (int)(rel[2] >> 31) + (int)(rel[3] >> 31);
+   // fold(): the mean of a 360-degree sample's valid rays, halved, as
+   // 0.5 * (sa (w0 + w1) + sb (w2 + w3)) with sa, sb = 1/2 for two valid rays
+   // (scaling by powers of two is exact, so this rounds like fold)
+   const float sa = (rel[0] >> 31) + (rel[1] >> 31) == 2 ? 0.5f : 1.f;
+   const float sb = (rel[2] >> 31) + (rel[3] >> 31) == 2 ? 0.5f : 1.f;
+   const unsigned long long sa2 = f2_pack(sa, sa), sb2 = f2_pack(sb, sb), half2 = f2_pack(0.5f, 0.5f);
+   // frames of quad (plane, local): b0 + stride * j
+   const int stride = qm.plane >= 0 ? 1 : qm.L;
 
    for (int t = 0; t < nq; ++t) {
       if (t + 1 < nq) {
@@ -294,19 +297,25 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
       __syncthreads();  // every thread's copies of quad t have landed
       if (act) {
          const uint32_t sb = sbase + (uint32_t)(t & 1) * stage_bytes;
-         float4 w[4];
+         ulonglong2 w[4];
 #pragma unroll
          for (int s = 0; s < 4; ++s)
             w[s] = (rel[s] >> 31) ? bilinear4_smem(sb + (rel[s] & 0xFFFFu) * 16u, ((rel[s] >> 20) & 0xFFu) * 16u,
-                                                   u[s], v[s])
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
-         const float r[4] = {fold(w[0].x, w[1].x, w[2].x, w[3].x, na, nb), fold(w[0].y, w[1].y, w[2].y, w[3].y, na, nb),
-                             fold(w[0].z, w[1].z, w[2].z, w[3].z, na, nb), fold(w[0].w, w[1].w, w[2].w, w[3].w, na, nb)};
-         const int q = k * qm.per_plane + first + t;
+                                                   u2[s], v2[s])
+                                  : make_ulonglong2(0ull, 0ull);
+         const unsigned long long r01 =
+             f2_mul(f2_add(f2_mul(f2_add(w[0].x, w[1].x), sa2), f2_mul(f2_add(w[2].x, w[3].x), sb2)), half2);
+         const unsigned long long r23 =
+             f2_mul(f2_add(f2_mul(f2_add(w[0].y, w[1].y), sa2), f2_mul(f2_add(w[2].y, w[3].y), sb2)), half2);
+         float r[4];
+         f2_unpack(r01, r[0], r[1]);
+         f2_unpack(r23, r[2], r[3]);
+         const int local = first + t;
+         const int b0 = qm.plane >= 0 ? 4 * local : k + qm.L * 4 * local;
 #pragma unroll
          for (int j = 0; j < 4; ++j) {
-            const int bf = quad_frame(qm, q, j);
-            if (bf >= 0) par[(size_t)bf * no + o] = r[j];
+            const int bf = b0 + stride * j;
+            if (bf < qm.batch) par[(size_t)bf * no + o] = r[j];
          }
       }
       __syncthreads();  // stage t & 1 is refilled with quad t + 2 next
