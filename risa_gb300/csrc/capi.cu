@@ -174,10 +174,10 @@ struct risa_gb_fan2para {
 // The engine's rebinning from frame quads stages each output tile's fan boxes
 // in shared memory; without boxes that fit, it gathers from global memory.
 static risa_gb_status prepare_f2p_staged(risa_gb_fan2para* h) {
-   std::vector<F2PGather> planes;
-   RG_TRY(build_f2p_gather_all(h->g, h->p, &planes));
-   std::vector<uint32_t> pk;
-   for (auto& t : planes) pk.insert(pk.end(), t.packed.begin(), t.packed.end());
+   // the gather table as uploaded by risa_gb_fan2para_create
+   std::vector<uint32_t> pk(h->packed.bytes / sizeof(uint32_t));
+   if (pk.empty()) return RISA_GB_OK;
+   RG_CUDA(cudaMemcpy(pk.data(), h->packed.p, h->packed.bytes, cudaMemcpyDeviceToHost));
    F2PStaged st;
    build_f2p_staged(pk.data(), h->g.L, h->g.Pf, h->g.Df, h->g.Pp, h->g.Dp, &st);
    if (st.stage_entries <= 0) return RISA_GB_OK;
@@ -1203,11 +1203,36 @@ risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, fl
       }
       h->slot_plane = plane;
    }
-   const int chunks = (n_frames + B - 1) / B;
-   for (int c = 0; c < chunks; ++c) {
-      const int slot = c & 1;
-      const int first = c * B;
-      const int nb = std::min(B, n_frames - first);
+   // Chunk sizes: a ramp of B/16 and B/4 frames at both ends, full chunks of
+   // B between. Nothing overlaps the first chunk's upload and the last one's
+   // download, so short end chunks shorten the pipeline's fill and drain.
+   // Every chunk but the last starts the next one on a plane-0 frame.
+   const int unit = plane == RISA_GB_PLANES_INTERLEAVED ? g.L : 1;
+   auto units = [&](int x) { return std::max(unit, x / unit * unit); };
+   const int r1 = std::min(B, units(B / 16)), r2 = std::min(B, units(B / 4));
+   std::vector<int> sizes;
+   {
+      const int odd = n_frames % unit;  // frames after the last whole plane group go with the last chunk
+      int left = n_frames - odd;
+      auto push = [&](int nb) {
+         nb = std::min(nb, left);
+         if (nb > 0) sizes.push_back(nb), left -= nb;
+      };
+      push(r1);
+      push(r2);
+      while (left > B + r2 + r1) push(B);
+      if (left > r2 + r1) push(left - r2 - r1);
+      push(r2);
+      push(r1);
+      if (odd) {
+         if (!sizes.empty() && sizes.back() + odd <= B) sizes.back() += odd;
+         else sizes.push_back(odd);
+      }
+   }
+   int first = 0;
+   for (size_t c = 0; c < sizes.size(); ++c) {
+      const int slot = (int)(c & 1);
+      const int nb = sizes[c];
       // slot buffers are reused every second chunk: wait for their last readers
       RG_CUDA(cudaStreamWaitEvent(h->s_h2d, h->ev_comp[slot], 0));
       RG_CUDA(cudaMemcpyAsync(h->raw_slot[slot].p, host_raw + (size_t)first * fs,
@@ -1215,7 +1240,7 @@ risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, fl
       RG_CUDA(cudaEventRecord(h->ev_h2d[slot], h->s_h2d));
       RG_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_h2d[slot], 0));
       RG_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_d2h[slot], 0));
-      // a chunk starting at a multiple of B keeps the interleaved plane phase
+      // every chunk starts on a plane-0 frame, so a full chunk replays the slot's graph
       if (nb == B) {
          RG_CUDA(cudaGraphLaunch(h->slot_exec[slot], h->s_comp));
       } else {
@@ -1227,6 +1252,7 @@ risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, fl
       RG_CUDA(cudaMemcpyAsync(host_img + (size_t)first * is, h->img_slot[slot].p, sizeof(float) * is * nb,
                               cudaMemcpyDeviceToHost, h->s_d2h));
       RG_CUDA(cudaEventRecord(h->ev_d2h[slot], h->s_d2h));
+      first += nb;
    }
    RG_CUDA(cudaStreamSynchronize(h->s_d2h));
    RG_CUDA(cudaStreamSynchronize(h->s_comp));
