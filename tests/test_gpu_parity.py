@@ -345,8 +345,8 @@ def test_fbp_fused_filter_staging():
 
 
 def test_graph_replay_and_host_path_match_enqueue():
-    d, sc, g, p, op = _fbp_case(rg.QUIRKS_NONE, True, True, L=2, frames=4)
-    n = sc.raw.shape[0]  # 8 frames
+    d, sc, g, p, op = _fbp_case(rg.QUIRKS_NONE, True, True, L=2, frames=8)
+    n = sc.raw.shape[0]  # 16 frames: host-path chunks 2, 2, 4, 4, 2, 2 (ramp, two graph replays, ramp)
     B = 4
     fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=B)
     N = d["n_pixels"]
@@ -370,6 +370,13 @@ def test_graph_replay_and_host_path_match_enqueue():
     himg2 = torch.zeros((n - 2, N, N), dtype=torch.float32).pin_memory()
     fbp.run_host(hraw[: n - 2], himg2, n - 2, rg.PLANES_INTERLEAVED)
     np.testing.assert_array_equal(himg2.numpy(), expect[: n - 2])
+    # an odd frame count: the last chunk takes the plane-0 frame left over, which
+    # the filter transforms without a partner slice (so not the same bits)
+    himg3 = torch.zeros((n - 1, N, N), dtype=torch.float32).pin_memory()
+    fbp.run_host(hraw[: n - 1], himg3, n - 1, rg.PLANES_INTERLEAVED)
+    got3 = himg3.numpy()
+    np.testing.assert_array_equal(got3[: n - 2], expect[: n - 2])
+    assert rel_err(got3[n - 2], expect[n - 2])[0] < MAX_REL
 
 
 def test_errors_are_reported():
