@@ -232,10 +232,12 @@ struct risa_gb_backprojection {
    DevBuf rowbase, colbase;  // adjoint: (hi, lo) line starts [Pp][N]
    DevBuf adj;               // adjoint: slice-interleaved image copies (reserve_adjoint)
    DevBuf tile_win;          // staged variants: window start + origin per tile and angle
+   std::vector<float> a_host, b_host;  // the staged variants' kernel-parameter copies of a and b
    BPCfg cfg(bool fused_mask) const {
       BPCfg c;
       c.Pp = g.Pp; c.Dp = g.Dp; c.N = g.N;
       c.a = a.as<float>(); c.b = b.as<float>(); c.t0 = t0.as<double>();
+      c.a_host = a_host.data(); c.b_host = b_host.data();
       c.ad = ad.as<double>(); c.bd = bd.as<double>();
       c.norm = norm;
       c.masking = fused_mask ? 1 : 0;
@@ -759,6 +761,8 @@ risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* gi, const r
    build_bp_tables(h->g, h->p, &t);
    RG_TRY(h->a.upload(t.a));
    RG_TRY(h->b.upload(t.b));
+   h->a_host = t.a;
+   h->b_host = t.b;
    RG_TRY(h->t0.upload(t.t0));
    RG_TRY(h->ad.upload(t.ad));
    RG_TRY(h->bd.upload(t.bd));

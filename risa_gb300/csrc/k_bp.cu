@@ -32,6 +32,7 @@ enum VariantKind { kTile, kPairs, kAsync, kAsyncPacked };
 struct BPVariant {
    int kind, slices, achunk, ppt;  // ppt: pixels per thread of the staged kernels
    const char* name;
+   bool cp = false;  // staged: angle coefficients from the constant bank (at most kCPAngles angles)
 };
 constexpr BPVariant kVariants[] = {
     {kPairs, 2, 32, 4, "pairs_s2_a32"},
@@ -53,6 +54,9 @@ constexpr BPVariant kVariants[] = {
     {kAsync, 4, 4, 4, "staged_s4_a4_p4"},
     {kAsync, 2, 8, 4, "staged_s2_a8_p4"},
     {kAsync, 4, 16, 8, "staged_s4_a16_p8"},
+    {kAsync, 4, 8, 4, "staged_cp_s4_a8_p4", true},
+    {kAsync, 4, 16, 4, "staged_cp_s4_a16_p4", true},
+    {kAsync, 2, 16, 4, "staged_cp_s2_a16_p4", true},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -457,18 +461,30 @@ __device__ __forceinline__ void stage_barrier(int id, bool wait) {
    }
 }
 
-template <int S, int ACH, bool PACKED, int PPT, int NST>
-__global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __restrict__ pairs,
-                                                              float* __restrict__ img, BPCfg cfg, int wlen,
-                                                              int batch) {
+// CP: the angle coefficients a, b of every angle travel in the kernel's
+// parameter space (16 KB, read through the constant cache, which uses none
+// of the shared-memory data path the backprojection is bound by); only the
+// tile's window-relative coordinate of each angle stays in shared memory,
+// four angles per broadcast load.
+struct BPAngleParams {
+   float a[kCPAngles], b[kCPAngles];
+};
+struct BPNoAngleParams {};
+
+template <int S, int ACH, bool PACKED, int PPT, int NST, bool CP>
+__global__ void __launch_bounds__(1024 / PPT)
+    bp_linear_async(const float4* __restrict__ pairs, float* __restrict__ img, BPCfg cfg, int wlen, int batch,
+                    const __grid_constant__ std::conditional_t<CP, BPAngleParams, BPNoAngleParams> ap) {
    static_assert(NST >= 2 && NST <= 4, "2 to 4 stages (one named barrier each)");
+   static_assert(!CP || ACH % 4 == 0, "window coordinates are read four angles at a time");
    constexpr int T = 32, H = S / 2, NT = 1024 / PPT, RS = NT / 32;  // RS: rows between a thread's pixels
    extern __shared__ float4 wsm[];  // [NST][ACH][H][wlen]
    __shared__ uint64_t full[NST];
    // per angle of a chunk: (a, b, window-relative coordinate, unused), read
    // with one broadcast 16-byte load per angle (three 4-byte loads cost 8% of
-   // the shared-memory wavefronts of the backprojection)
-   __shared__ float4 s_par[NST][ACH];
+   // the shared-memory wavefronts of the backprojection); with CP only the
+   // coordinates, four angles per float4
+   __shared__ float4 s_par[NST][CP ? ACH / 4 : ACH];
    __shared__ volatile int s_fail;
    __shared__ int s_break;
 
@@ -543,7 +559,11 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
    };
    auto commit = [&](int ch, int st, const Prep& r) {
       const int na = min(ACH, Pp - ch * ACH);
-      if (lane < na) s_par[st][lane] = r.par;
+      if (CP) {
+         if (lane < ACH) reinterpret_cast<float*>(&s_par[st][0])[lane] = lane < na ? r.par.z : 0.f;
+      } else if (lane < na) {
+         s_par[st][lane] = r.par;
+      }
       __syncwarp();
       if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)(na * H) * plane_bytes);
       __syncwarp();
@@ -606,9 +626,8 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
       const uint32_t sbase = wbase + (uint32_t)(st * ACH * H) * plane_bytes;
       // one angle of the chunk; CHECK: skip the pixel steps whose block is
       // outside the circle (warp-uniform), otherwise straight-line code
-      auto angle = [&](int ai, auto check) {
+      auto angle = [&](int ai, const float4 q, auto check) {
          constexpr bool CHECK = decltype(check)::value;
-         const float4 q = s_par[st][ai];
          const float a = q.x, b = q.y;
          const float t0 = q.z + (float)xo * a + (float)yo * b;
          const float step = (float)RS * b;
@@ -653,11 +672,28 @@ __global__ void __launch_bounds__(1024 / PPT) bp_linear_async(const float4* __re
             }
          }
       };
-      if (live == (1u << PPT) - 1u) {
-#pragma unroll 2
-         for (int ai = 0; ai < na; ++ai) angle(ai, std::false_type{});
+      if constexpr (CP) {
+         // four angles per window-coordinate load; a, b from the parameter space
+         auto quad = [&](int a4, auto check) {
+            const float4 r4 = s_par[st][a4 >> 2];
+            const int ang = ch * ACH + a4;
+            angle(a4, make_float4(ap.a[ang], ap.b[ang], r4.x, 0.f), check);
+            if (a4 + 1 < na) angle(a4 + 1, make_float4(ap.a[ang + 1], ap.b[ang + 1], r4.y, 0.f), check);
+            if (a4 + 2 < na) angle(a4 + 2, make_float4(ap.a[ang + 2], ap.b[ang + 2], r4.z, 0.f), check);
+            if (a4 + 3 < na) angle(a4 + 3, make_float4(ap.a[ang + 3], ap.b[ang + 3], r4.w, 0.f), check);
+         };
+         if (live == (1u << PPT) - 1u) {
+            for (int a4 = 0; a4 < na; a4 += 4) quad(a4, std::false_type{});
+         } else {
+            for (int a4 = 0; a4 < na; a4 += 4) quad(a4, std::true_type{});
+         }
       } else {
-         for (int ai = 0; ai < na; ++ai) angle(ai, std::true_type{});
+         if (live == (1u << PPT) - 1u) {
+#pragma unroll 2
+            for (int ai = 0; ai < na; ++ai) angle(ai, s_par[st][ai], std::false_type{});
+         } else {
+            for (int ai = 0; ai < na; ++ai) angle(ai, s_par[st][ai], std::true_type{});
+         }
       }
       // Release the stage: the other warps arrive on named barrier
       // 1 + ch % NST without waiting and go on with the stages already
@@ -713,8 +749,9 @@ inline size_t async_smem(int S, int ach, int wlen, int nst = 2) {
    return (size_t)nst * sizeof(float2) * (size_t)S * ach * wlen;
 }
 
-template <int S, int ACH, bool PACKED, int PPT, int NST = 2>
+template <int S, int ACH, bool PACKED, int PPT, int NST = 2, bool CP = false>
 cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& cfg, cudaStream_t st) {
+   if (CP && (cfg.Pp > kCPAngles || !cfg.a_host || !cfg.b_host)) return cudaErrorInvalidConfiguration;
    const int wlen = window_len(cfg.scale, 32, 32);
    const size_t smem = async_smem(S, ACH, wlen, NST);
    if (smem > kMaxPairsSmem) return cudaErrorInvalidConfiguration;
@@ -731,26 +768,31 @@ cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& 
       if (e != cudaSuccess) return e;
    }
    if (cfg.mid_event && (e = cudaEventRecord(cfg.mid_event, st)) != cudaSuccess) return e;
-   auto kern = bp_linear_async<S, ACH, PACKED, PPT, NST>;
+   auto kern = bp_linear_async<S, ACH, PACKED, PPT, NST, CP>;
    if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
    }
    dim3 grid((cfg.N + 31) / 32, (cfg.N + 31) / 32, groups);
-   kern<<<grid, 1024 / PPT, smem, st>>>(reinterpret_cast<const float4*>(cfg.pairs), img, cfg, wlen, batch);
+   std::conditional_t<CP, BPAngleParams, BPNoAngleParams> ap{};
+   if constexpr (CP) {
+      std::memcpy(ap.a, cfg.a_host, sizeof(float) * cfg.Pp);
+      std::memcpy(ap.b, cfg.b_host, sizeof(float) * cfg.Pp);
+   }
+   kern<<<grid, 1024 / PPT, smem, st>>>(reinterpret_cast<const float4*>(cfg.pairs), img, cfg, wlen, batch, ap);
    return cudaGetLastError();
 }
 
-template <int S, bool PACKED, int PPT>
+template <int S, bool PACKED, int PPT, bool CP = false>
 cudaError_t launch_async_fit(const float* sino, float* img, int batch, const BPCfg& cfg, int ach,
                              cudaStream_t st) {
    const int wlen = window_len(cfg.scale, 32, 32);
    while (ach > 4 && async_smem(S, ach, wlen) > kMaxPairsSmem) ach /= 2;
    switch (ach) {
-      case 32: return launch_async<S, 32, PACKED, PPT>(sino, img, batch, cfg, st);
-      case 16: return launch_async<S, 16, PACKED, PPT>(sino, img, batch, cfg, st);
-      case 8: return launch_async<S, 8, PACKED, PPT>(sino, img, batch, cfg, st);
-      default: return launch_async<S, 4, PACKED, PPT>(sino, img, batch, cfg, st);
+      case 32: return launch_async<S, 32, PACKED, PPT, 2, CP>(sino, img, batch, cfg, st);
+      case 16: return launch_async<S, 16, PACKED, PPT, 2, CP>(sino, img, batch, cfg, st);
+      case 8: return launch_async<S, 8, PACKED, PPT, 2, CP>(sino, img, batch, cfg, st);
+      default: return launch_async<S, 4, PACKED, PPT, 2, CP>(sino, img, batch, cfg, st);
    }
 }
 
@@ -1051,6 +1093,9 @@ cudaError_t launch_backprojection(const float* sino, float* img, int batch, cons
    if (v.kind == kAsync || v.kind == kAsyncPacked) {
       const bool pk = v.kind == kAsyncPacked;
       const int ach = v.achunk;
+      if (v.cp)
+         return v.slices == 2 ? launch_async_fit<2, false, 4, true>(sino, img, batch, cfg, ach, st)
+                              : launch_async_fit<4, false, 4, true>(sino, img, batch, cfg, ach, st);
       if (v.ppt == 8) {
          if (v.slices == 2)
             return pk ? launch_async_fit<2, true, 8>(sino, img, batch, cfg, ach, st)

@@ -238,6 +238,7 @@ cudaError_t launch_filter_taps_grad(const float* x, const float* g, int batch, c
                                     cudaStream_t st);
 
 // ---------------------------------------------------------------- backprojection
+constexpr int kCPAngles = 2048;  // angles the backprojection can take from its kernel parameters
 struct BPCfg {
    int Pp, Dp, N;
    const float* a;      // [Pp]
@@ -260,6 +261,8 @@ struct BPCfg {
    // the backprojection kernel (timing of the two separately)
    cudaEvent_t mid_event = nullptr;
    bool prefilled = false;  // staged variants: the pair records are already written (launch_filter_pairs)
+   const float* a_host = nullptr;  // host copies of a and b (the staged variants' constant-bank angle
+   const float* b_host = nullptr;  // coefficients, at most kCPAngles angles)
    const int2* tile_win = nullptr;  // staged variants: per tile and angle (window start, bits of the float
                                     // coordinate of the tile origin in it), bp_tile_windows; else FP64 on device
    void* adj_scratch = nullptr;  // adjoint: slice-interleaved image copies (bp_adjoint_scratch_bytes)
