@@ -41,10 +41,11 @@ FRAMES_PER_PLANE = 2000
 FLOPS_PER_UPDATE = 6  # ray coordinate FMA (2) + weight add (1) + interpolation FMA (2) + accumulate (1)
 SMEM_BYTES_PER_UPDATE = 8  # one FP32 (midpoint, difference) pair per pixel x angle and slice
 SMEM_BYTES_PER_CLK_SM = 128  # nominal shared-memory bandwidth per SM
-# dram__bytes_read.sum + dram__bytes_write.sum of a 64-slice backprojection launch
-# (profiles/bp_staged_fbp512_ncu.txt): the pair records read once and the images
-# written, both proportional to the slices, so a launch of B slices moves B/64 of it
-BP_DRAM_BYTES_PER_SLICE = 740.4e6 / 64
+# dram__bytes_read.sum + dram__bytes_write.sum of a 64-slice launch of the autotuned
+# backprojection variant (staged_cp_s4_a8_p4, profiles/bp_staged_fbp512_ncu.txt):
+# the pair records read once and the images written, both proportional to the
+# slices, so a launch of B slices moves B/64 of it
+BP_DRAM_BYTES_PER_SLICE = 727.8e6 / 64
 WORKLOAD_NAME = ("full-rate streaming: 2 planes x 2000 frames of 1000x1152 uint16 fan sinograms, 1% defective "
                  "detectors -> 1024x1024 parallel (pad 2048, Shepp-Logan) -> 512^2 FP32, circular mask")
 
