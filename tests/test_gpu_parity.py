@@ -311,6 +311,32 @@ def test_fbp_staged_rebinning():
             assert mr < MAX_REL and l2 < MAX_REL, (plane, b, mr, l2)
 
 
+def test_fbp_long_filter_rows():
+    """Filter length 2048 (1024 rays zero padded, the benchmark's length):
+    the engine's filter pass with one row pair per 128-thread CTA writing the
+    pair records; an even and an odd batch (the last pair without its second
+    slice), both plane modes."""
+    d, sc, g, p, op = _fbp_case(rg.QUIRKS_NONE, True, masking=True, L=2, frames=3)
+    d.update(n_par_proj=96, n_par_det=1024, n_pixels=128)
+    g = geom(d)
+    n = sc.raw.shape[0]
+    oref, odark = oracle.attenuation_init(sc.ref, sc.dark, 2, 0.67, 1.5, True, rg.QUIRKS_NONE)
+    rec = oracle.f2p_records(ns(d), rg.QUIRKS_NONE)
+    fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=n)
+    raw = sc.raw.view(np.int16)
+    N = d["n_pixels"]
+    plane0 = np.flatnonzero(sc.planes == 0)
+    for plane, idx in ((rg.PLANES_INTERLEAVED, np.arange(n)), (rg.PLANES_INTERLEAVED, np.arange(n - 2)),
+                       (0, plane0)):
+        exp = oracle.fbp(ns(d), op, rec, oref, odark, sc.raw[idx], sc.planes[idx])
+        img = torch.empty((len(idx), N, N), dtype=torch.float32, device="cuda")
+        fbp.enqueue(dev(raw[idx]), img, plane, len(idx))
+        got = host(img)
+        for b in range(len(idx)):
+            mr, l2 = rel_err(got[b], exp[b])
+            assert mr < MAX_REL and l2 < MAX_REL, (plane, len(idx), b, mr, l2)
+
+
 def test_fbp_fused_filter_staging():
     """Staged backprojection variants with a radix-16 filter length: the filter
     writes the pair records itself (no staging pass); an odd batch leaves the
