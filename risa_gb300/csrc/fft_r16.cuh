@@ -8,8 +8,24 @@ namespace fft {
 
 constexpr float kSqrtHalf = 0.70710678118654752f;
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// complex add and subtract as one f32x2 instruction each (each lane rounded
+// like the scalar add.rn / sub.rn)
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+   float2 r;
+   asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+       "add.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n\t}"
+       : "=f"(r.x), "=f"(r.y)
+       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+   return r;
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+   float2 r;
+   asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+       "sub.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n\t}"
+       : "=f"(r.x), "=f"(r.y)
+       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+   return r;
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
