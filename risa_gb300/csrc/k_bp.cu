@@ -953,15 +953,16 @@ __global__ void __launch_bounds__(128) bp_adjoint_rows(const float4* __restrict_
    // FP32 error of jlo, ~1e-4 at these sizes), each then tested exactly.
    const float lo_num = s_hi > 0.f ? -1.f : 1.f;
    const int ncand = (int)floorf(2.f * fabsf(inv) + 0.002f) + 1;
-   float acc[8];
-#pragma unroll
-   for (int s = 0; s < 8; ++s) acc[s] = 0.f;
+   // the 8 slices of a pixel as four f32x2 pairs: one fma.rn.f32x2 per pair
+   // (each lane rounded like fmaf)
+   unsigned long long acc2[4] = {0ull, 0ull, 0ull, 0ull};
+   const ulonglong2* imp = reinterpret_cast<const ulonglong2*>(im);
    for (int r = 0; r < N; ++r) {
       const float2 hb = s_line[r];
       const float t_hi = hb.x - kf, t_lo = hb.y;
       const float jlo = (lo_num - (t_hi + t_lo)) * inv;
       const int j1 = (int)ceilf(jlo - 1e-3f);
-      const float4* row = im + (size_t)r * N * 2;
+      const ulonglong2* row = imp + (size_t)r * N * 2;
       for (int c = 0; c < ncand; ++c) {
          const int j = j1 + c;
          if ((unsigned)j >= (unsigned)N) continue;
@@ -969,18 +970,18 @@ __global__ void __launch_bounds__(128) bp_adjoint_rows(const float4* __restrict_
          const float d = fabsf(fmaf(jf, s_hi, t_hi) + fmaf(jf, s_lo, t_lo));
          if (d < 1.f) {
             const float w = 1.f - d;
-            const float4 v0 = __ldg(row + 2 * j), v1 = __ldg(row + 2 * j + 1);
-            acc[0] = fmaf(w, v0.x, acc[0]);
-            acc[1] = fmaf(w, v0.y, acc[1]);
-            acc[2] = fmaf(w, v0.z, acc[2]);
-            acc[3] = fmaf(w, v0.w, acc[3]);
-            acc[4] = fmaf(w, v1.x, acc[4]);
-            acc[5] = fmaf(w, v1.y, acc[5]);
-            acc[6] = fmaf(w, v1.z, acc[6]);
-            acc[7] = fmaf(w, v1.w, acc[7]);
+            const unsigned long long w2 = f2_pack(w, w);
+            const ulonglong2 v0 = __ldg(row + 2 * j), v1 = __ldg(row + 2 * j + 1);
+            acc2[0] = f2_fma(w2, v0.x, acc2[0]);
+            acc2[1] = f2_fma(w2, v0.y, acc2[1]);
+            acc2[2] = f2_fma(w2, v1.x, acc2[2]);
+            acc2[3] = f2_fma(w2, v1.y, acc2[3]);
          }
       }
    }
+   float acc[8];
+#pragma unroll
+   for (int q = 0; q < 4; ++q) f2_unpack(acc2[q], acc[2 * q], acc[2 * q + 1]);
 #pragma unroll
    for (int s = 0; s < 8; ++s)
       if (8 * g + s < batch) sino[((size_t)(8 * g + s) * cfg.Pp + i) * cfg.Dp + k] = acc[s] * cfg.norm;
