@@ -215,6 +215,21 @@ risa_gb_status risa_gb_fan2para_destroy(risa_gb_fan2para* h);
 risa_gb_status risa_gb_fan2para_tables_host(const risa_gb_geometry* g, const risa_gb_params* p,
                                             int plane, uint32_t* packed, float* u, float* v);
 
+/* Host-only build of the batched engine's staged rebinning tables (no GPU
+ * needed; no counterpart in the reference, whose interpolation kernel
+ * gathers straight from global memory). Outputs are cut into tiles of 8
+ * angles x 32 rays (tile t = angle_tile * ceil(Dp/32) + ray_tile); for every
+ * plane, tile and slot, boxes[((plane*tiles + t)*4 + slot)*4 + 0..3] = (first
+ * fan row, first fan column, rows, columns) of the circular box the slot's
+ * bilinear taps touch; rel[(plane*4 + slot)*Pp*Dp + o] = valid<<31 |
+ * row_pitch<<20 | entry of the output's first tap, counting the tile's four
+ * boxes one after the other with rows row_pitch entries apart. Arrays hold
+ * L*tiles*16 and L*4*Pp*Dp entries. *stage_entries = the most entries of one
+ * tile's boxes, 0 when the geometry is not staged (the engine then gathers
+ * from global memory). */
+risa_gb_status risa_gb_fan2para_staged_tables_host(const risa_gb_geometry* g, const risa_gb_params* p,
+                                                   int32_t* boxes, uint32_t* rel, int* stage_entries);
+
 /* ---------------------------------------------------------------------------
  * Filter (Filter.cu:102-191, applyFilter :231-241). Row-wise ramp-family
  * filtering of parallel sinograms with this library's own FFT (no cuFFT),

@@ -98,6 +98,7 @@ SIGNATURES = {
     "risa_gb_fan2para_enqueue_adjoint": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
     "risa_gb_fan2para_destroy": (_i, [_vp]),
     "risa_gb_fan2para_tables_host": (_i, [_vp, _vp, _i, _vp, _vp, _vp]),
+    "risa_gb_fan2para_staged_tables_host": (_i, [_vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_int)]),
     "risa_gb_filter_create": (_i, [_vp, _vp, _pp]),
     "risa_gb_filter_enqueue": (_i, [_vp, _vp, _i, _vp]),
     "risa_gb_filter_response": (_i, [_vp, ctypes.POINTER(ctypes.c_int), _vp]),
@@ -380,6 +381,21 @@ def fan2para_tables_host(geom: Geometry, params: Params, plane: int = 0):
     _check(lib().risa_gb_fan2para_tables_host(ctypes.byref(geom), ctypes.byref(params), plane, ptr(pk),
                                               ptr(u), ptr(v)), "fan2para_tables_host")
     return pk.reshape(4, -1), u.reshape(4, -1), v.reshape(4, -1)
+
+
+def fan2para_staged_tables_host(geom: Geometry, params: Params):
+    """The engine's staged rebinning tables (host build, no GPU): (boxes
+    [L, tiles, 4 slots, 4] as (first row, first column, rows, columns), rel
+    [L, 4, Pp*Dp], stage_entries); stage_entries 0 when not staged."""
+    import numpy as np
+    L, Pp, Dp = geom.n_planes, geom.n_par_proj, geom.n_par_det
+    tiles = ((Pp + 7) // 8) * ((Dp + 31) // 32)
+    boxes = np.zeros((L, tiles, 4, 4), np.int32)
+    rel = np.zeros((L, 4, Pp * Dp), np.uint32)
+    se = ctypes.c_int(0)
+    _check(lib().risa_gb_fan2para_staged_tables_host(ctypes.byref(geom), ctypes.byref(params), ptr(boxes),
+                                                     ptr(rel), ctypes.byref(se)), "fan2para_staged_tables_host")
+    return boxes, rel, se.value
 
 
 class Filter(_Handle):

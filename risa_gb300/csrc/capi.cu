@@ -511,6 +511,27 @@ risa_gb_status risa_gb_fan2para_tables_host(const risa_gb_geometry* gi, const ri
    return RISA_GB_OK;
 }
 
+risa_gb_status risa_gb_fan2para_staged_tables_host(const risa_gb_geometry* gi, const risa_gb_params* pi,
+                                                   int32_t* boxes, uint32_t* rel, int* stage_entries) {
+   Geometry g;
+   Params p;
+   RG_TRY(import_geometry(gi, &g, true, true, false));
+   RG_TRY(import_params(pi, &p));
+   if (!boxes || !rel || !stage_entries) return fail(RISA_GB_EINVAL, "null output");
+   std::vector<F2PGather> planes;
+   RG_TRY(build_f2p_gather_all(g, p, &planes));
+   std::vector<uint32_t> pk;
+   for (auto& t : planes) pk.insert(pk.end(), t.packed.begin(), t.packed.end());
+   F2PStaged st;
+   build_f2p_staged(pk.data(), g.L, g.Pf, g.Df, g.Pp, g.Dp, &st);
+   *stage_entries = st.stage_entries;
+   if (st.stage_entries > 0) {
+      std::memcpy(boxes, st.boxes.data(), sizeof(int4) * st.boxes.size());
+      std::memcpy(rel, st.rel.data(), sizeof(uint32_t) * st.rel.size());
+   }
+   return RISA_GB_OK;
+}
+
 risa_gb_status risa_gb_fan2para_create(const risa_gb_geometry* gi, const risa_gb_params* pi,
                                        risa_gb_fan2para** out) {
    if (!out) return fail(RISA_GB_EINVAL, "out is NULL");
