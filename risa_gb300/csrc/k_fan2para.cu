@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "async_copy.h"
 #include "f32x2.cuh"
 #include "kernels.h"
 
@@ -176,14 +177,6 @@ constexpr int kStageSlotsPerThread = kF2PMaxStageEntries / kStageThreads;
 constexpr int kStageQuadsPerCTA = 32;
 static_assert(kStageThreads == 256, "one warp per tile angle");
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
-   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 
 __device__ __forceinline__ ulonglong2 lds128_pairs(uint32_t addr) {
    ulonglong2 v;
@@ -262,8 +255,8 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
       const uint32_t dst = sbase + (uint32_t)(t & 1) * stage_bytes + threadIdx.x * 16u;
 #pragma unroll
       for (int i = 0; i < kStageSlotsPerThread; ++i)
-         if (goff[i] >= 0) cp_async16(dst + (uint32_t)i * (kStageThreads * 16u), src + goff[i]);
-      cp_async_commit();
+         if (goff[i] >= 0) async::cp_async_cg16(dst + (uint32_t)i * (kStageThreads * 16u), src + goff[i]);
+      async::cp_async_commit();
    };
    if (nq > 0) stage(0);
 
@@ -290,9 +283,9 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
    for (int t = 0; t < nq; ++t) {
       if (t + 1 < nq) {
          stage(t + 1);
-         cp_async_wait<1>();
+         async::cp_async_wait<1>();
       } else {
-         cp_async_wait<0>();
+         async::cp_async_wait<0>();
       }
       __syncthreads();  // every thread's copies of quad t have landed
       if (act) {
