@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--frames", type=int, default=FRAMES_PER_PLANE, help="frames per plane")
-    ap.add_argument("--batch", type=int, default=256, help="frames per engine chunk (multiple of 2)")
+    ap.add_argument("--batch", type=int, default=512, help="frames per engine chunk (multiple of 2)")
     ap.add_argument("--distinct", type=int, default=8, help="distinct synthetic frames per plane")
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/roofline/cpu legs")
     ap.add_argument("--bp-variant", type=int, default=-1,
