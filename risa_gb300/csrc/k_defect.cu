@@ -66,16 +66,18 @@ __global__ void __launch_bounds__(kStatThreads) defect_stats(const uint16_t* __r
 // Detector-major frames with D % 8 == 0 and 16-byte aligned rows: each thread
 // takes 8 adjacent columns (one 16-byte load per row), keeps their max/min as
 // packed 16-bit pairs and their total variation in 32 bits (at most
-// kStatRowsVec * 65535 per chunk), and adds the chunk's results atomically.
-// Rows are loaded kStatBatch at a time so that many loads are in flight.
-constexpr int kStatRowsVec = 64;
+// `rows` * 65535 per chunk, rows <= 32768), and adds the chunk's results
+// atomically. Rows are loaded kStatBatch at a time so that many loads are in
+// flight. Each chunk ends in 6 atomics per column, so large batches take
+// longer chunks (fewer atomics) while the grid stays large (the launcher).
+constexpr int kStatRowsVec = 64;  // shortest chunk
 constexpr int kStatBatch = 8;
 __global__ void __launch_bounds__(256) defect_stats_vec8(const uint16_t* __restrict__ frames,
-                                                         ColStats* __restrict__ st, int P, int D) {
+                                                         ColStats* __restrict__ st, int P, int D, int rows) {
    const int o = blockIdx.x * blockDim.x + threadIdx.x;  // column octet
    if (8 * o >= D) return;
-   const int r0 = blockIdx.y * kStatRowsVec;
-   const int r1 = min(r0 + kStatRowsVec, P - 1);  // pairs (p, p+1) with p < r1
+   const int r0 = blockIdx.y * rows;
+   const int r1 = min(r0 + rows, P - 1);  // pairs (p, p+1) with p < r1
    if (r0 >= r1) return;
    const uint4* f = reinterpret_cast<const uint4*>(frames + (size_t)blockIdx.z * P * D) + o;
    const size_t rs = (size_t)D / 8;
@@ -315,8 +317,12 @@ cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const Defect
       // one block spans a frame's column octets where it can (D <= 2048)
       const int octets = cfg.D / 8;
       const int threads = std::min(256, (octets + 31) / 32 * 32);
-      dim3 grid((octets + threads - 1) / threads, (cfg.P - 1 + kStatRowsVec - 1) / kStatRowsVec, batch);
-      defect_stats_vec8<<<grid, threads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D);
+      // double the chunk while the grid keeps at least 1024 CTAs
+      int rows = kStatRowsVec;
+      auto ctas = [&](int r) { return (long long)batch * ((cfg.P - 1 + r - 1) / r) * ((octets + threads - 1) / threads); };
+      while (rows < cfg.P - 1 && rows < 32768 && ctas(2 * rows) >= 1024) rows *= 2;
+      dim3 grid((octets + threads - 1) / threads, (cfg.P - 1 + rows - 1) / rows, batch);
+      defect_stats_vec8<<<grid, threads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D, rows);
    } else {
       dim3 grid((cfg.D + kStatThreads - 1) / kStatThreads, (cfg.P - 1 + kStatRows - 1) / kStatRows,
                 batch);
