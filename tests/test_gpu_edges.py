@@ -96,3 +96,32 @@ def test_largest_sweep_geometry_staged():
     exp = oracle.mask(oracle.backproject(sino[0], N), 0.0)
     mr, l2 = rel_err(got[0], exp)
     assert mr < MAX_REL and l2 < MAX_REL, (rg.Backprojection.variant_name(v), mr, l2)
+
+
+def test_constant_parameter_variants_refuse_many_angles():
+    """The staged variants that take the angle coefficients from their kernel
+    parameters hold at most 2048 angles: with 2100 they refuse before any
+    launch (an error, the context stays usable) and the autotuner picks
+    another variant, whose output matches the oracle."""
+    Pp, Dp, N = 2100, 96, 64
+    g = rg.make_geometry(n_par_proj=Pp, n_par_det=Dp, n_pixels=N)
+    bp = rg.Backprojection(g, rg.make_params(masking=True))
+    bp.reserve(1)
+    names = [rg.Backprojection.variant_name(v) for v in range(rg.Backprojection.variant_count())]
+    cp = [v for v, name in enumerate(names) if name.startswith("staged_cp")]
+    assert cp
+    sino, _ = phantom.parallel_sinograms(1, Pp, Dp, 200.0, seed=5)
+    img = torch.empty((1, N, N), dtype=torch.float32, device="cuda")
+    for v in cp:
+        bp.set_variant(v)
+        with pytest.raises(rg.RisaError):
+            bp.enqueue(dev(sino), img, 1)
+    v = bp.autotune(dev(sino), img, 1)
+    assert v not in cp
+    img.fill_(np.nan)
+    bp.enqueue(dev(sino), img, 1)
+    got = host(img)
+    bp.check()
+    exp = oracle.mask(oracle.backproject(sino[0], N), 0.0)
+    mr, l2 = rel_err(got[0], exp)
+    assert mr < MAX_REL and l2 < MAX_REL, (names[v], mr, l2)
