@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kThreads) fan2para_gather_quads(const float4* 
 // fan2para_gather_quads, so the same bits.
 constexpr int kStageThreads = kF2PTileAngles * kF2PTileRays;  // one output per thread
 constexpr int kStageSlotsPerThread = kF2PMaxStageEntries / kStageThreads;
-constexpr int kStageQuadsPerCTA = 32;
+constexpr int kStageQuadsPerCTA = 64;
 static_assert(kStageThreads == 256, "one warp per tile angle");
 
 
