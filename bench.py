@@ -273,6 +273,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     line.update(extras)
     if "plain" in line:
         line["speedup_vs_plain"] = value / world / line["plain"]["value"]
+    if line.get("plain_reference", {}).get("value"):
+        line["speedup_vs_plain_reference"] = value / world / line["plain_reference"]["value"]
     if "roofline" in line and peaks:
         line["roofline"]["peaks_file"] = {k: peaks.get(k) for k in ("hbm_gbs", "sm_max_mhz")}
     print(json.dumps(line), flush=True)
@@ -330,7 +332,12 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     updates = B * inside * Pp
     # The backprojection kernel is bound by shared-memory bandwidth: every
     # update reads one FP32 (midpoint, difference) pair of its slice (8 B).
-    smem_peak = SMEM_BYTES_PER_CLK_SM * sms * sm_mhz * 1e6 / 1e9  # GB/s
+    # Denominators measured on this GPU (risa_gb_measure_peak), nominal beside.
+    smem_meas = rg.measure_peak(rg.PEAK_SMEM_READ, 5, stream)
+    fma_meas = rg.measure_peak(rg.PEAK_FP32_FMA, 5, stream)
+    smem_nominal = SMEM_BYTES_PER_CLK_SM * sms * sm_mhz * 1e6 / 1e9  # GB/s
+    smem_peak = smem_meas["value"]
+    fp32_peak_meas = fma_meas["value"]
     smem_gbs = updates * SMEM_BYTES_PER_UPDATE / (t_kern / 1e3) / 1e9
     bp_tflops = updates * FLOPS_PER_UPDATE / (t_kern / 1e3) / 1e12
     out["roofline"] = {
@@ -340,12 +347,18 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
         "traffic_source": "ncu capture of a 64-slice launch, scaled by slices per launch",
         "work": f"{SMEM_BYTES_PER_UPDATE} B of shared-memory reads per pixel x angle update and slice, "
                 f"{inside} in-circle pixels x {Pp} angles x {B} slices per launch",
-        "peak_source": f"nominal shared-memory bandwidth {SMEM_BYTES_PER_CLK_SM} B/clk/SM x {sms} SMs x "
-                       f"{sm_mhz:.0f} MHz (MEASURED_PEAKS.json carries no shared-memory figure)",
+        "peak_source": "measured: risa_gb_measure_peak(RISA_GB_PEAK_SMEM_READ), conflict-free 128-bit "
+                       f"shared loads on all {sms} SMs, {smem_meas['per_sm_per_clk']:.1f} B/clk/SM at "
+                       f"{smem_meas['sm_mhz']:.0f} MHz",
+        "peak_nominal": smem_nominal, "frac_nominal": smem_gbs / smem_nominal,
+        "peak_nominal_source": f"{SMEM_BYTES_PER_CLK_SM} B/clk/SM x {sms} SMs x {sm_mhz:.0f} MHz",
         "kernel_ms": t_kern, "staging_ms": t_stage,
-        "fp32": {"achieved": bp_tflops, "peak": fp32_peak, "unit": "TFLOP/s", "frac": bp_tflops / fp32_peak,
-                 "work": f"{FLOPS_PER_UPDATE} FLOP per update",
-                 "peak_source": f"nominal FFMA rate 128 lanes x 2 FLOP x {sms} SMs x {sm_mhz:.0f} MHz"},
+        "fp32": {"achieved": bp_tflops, "peak": fp32_peak_meas, "unit": "TFLOP/s",
+                 "frac": bp_tflops / fp32_peak_meas, "work": f"{FLOPS_PER_UPDATE} FLOP per update",
+                 "peak_source": "measured: risa_gb_measure_peak(RISA_GB_PEAK_FP32_FMA), "
+                                f"{fma_meas['per_sm_per_clk']:.1f} FLOP/clk/SM at {fma_meas['sm_mhz']:.0f} MHz",
+                 "peak_nominal": fp32_peak, "frac_nominal": bp_tflops / fp32_peak,
+                 "peak_nominal_source": f"128 FMA lanes x 2 FLOP x {sms} SMs x {sm_mhz:.0f} MHz"},
     }
     out["bp"] = {"gupdates_per_s": updates / (t_bp / 1e3) / 1e9,
                  "gupdates_per_s_kernel": updates / (t_kern / 1e3) / 1e9,
@@ -391,7 +404,13 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
         t_plain = time.perf_counter() - t0
     plain_value = n_plain / t_plain
     out["plain"] = {"value": plain_value, "unit": "slices/s", "frames": n_plain,
-                    "how": "one frame per stage launch, stream sync after each stage, device-resident input"}
+                    "how": "this library's stage kernels, one frame per stage launch, stream sync after each "
+                           "stage, device-resident input"}
+    try:
+        out["plain_reference"] = measure_plain_reference(torch, rg, sc, raw, g, stream, min(32, n))
+    except Exception as e:  # reported, never hides the headline line
+        out["plain_reference"] = {"error": f"{type(e).__name__}: {e}"}
+    out["bp"]["reference_kernel"] = out["plain_reference"].get("bp_gupdates_per_s")
 
     # ---- end to end through the host-buffer entry point
     hraw = torch.from_numpy(sc.raw.view(np.int16)).pin_memory()
@@ -430,6 +449,84 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
         except Exception as e:  # reported, never hides the headline line
             out[key] = {"error": f"{type(e).__name__}: {e}"}
     return out
+
+
+def measure_plain_reference(torch, rg, sc, raw, g, stream, n_frames: int) -> dict:
+    """The reference's own CUDA stages on the same workload: its stage sources
+    compiled for sm_103a (oracle/ref_harness) and launched as its processor()
+    loops launch them, one frame per stage launch with 16 x 16 blocks and a
+    stream sync after each stage, device-resident raw frames:
+      computeAttenuation (Attenuation.cu:158-161),
+      setValue + interpolation (Fan2Para.cu:220-238; RISA-mode tables in the
+        reference's layout, built by the oracle's pinned restatement of
+        computeFan2ParaTransp),
+      cuFFT R2C + applyFilter + C2R (Filter.cu:119-137; the reference filters
+        rows of length Dp = 1024 without zero padding, this library pads to 2048),
+      backProjectLinear (Backprojection.cu:187-189), mask (Masking.cu:134-135).
+    Defect repair is left out: the reference runs it on the host
+    (DetectorInterpolation.cu:113-139) and its pipeline does not wire it."""
+    from oracle import ref_kernels as rk
+    import oracle
+
+    why = rk.unavailable()
+    if why:
+        return {"unavailable": why}
+    w = dict(WORKLOAD, image_center_x=0.0, image_center_y=0.0)
+    L, Pf, Df, N = w["n_planes"], w["n_fan_proj"], w["n_fan_det"], w["n_pixels"]
+    Pp, Dp = w["n_par_proj"], w["n_par_det"]
+    dev = raw.device
+    torch.zeros(1, device=dev)  # the primary context is current for the driver API
+    rk.lib()
+    z = oracle.f2p_tables_risa(make_oracle_geom())
+    f2p_in = rk.fan2para_inputs(w, z, 16)
+    p_risa = rg.make_params(quirks=rg.QUIRKS_RISA, filter_type="sheppLogan", masking=True)
+    ref_avg, dark_avg = rg.Attenuation(g, p_risa, sc.ref, 1, sc.dark, 1).tables()
+    t_ref = torch.from_numpy(ref_avg).to(dev)
+    t_dark = torch.from_numpy(dark_avg).to(dev)
+    t_mask = torch.ones((Pf, Df), dtype=torch.float32, device=dev)
+    n_h, h = rg.Filter(g, p_risa).response()
+    assert n_h == Dp
+    t_h = torch.from_numpy(np.ascontiguousarray(np.asarray(h, np.float32))).to(dev)
+    sin_t, cos_t, norm, scale, center = rk.bp_setup(Pp, Dp, N, 0.0)
+    rk.bp_constants(sin_t, cos_t, Pp, norm, scale, center)
+    fan = torch.empty((Pf, Df), dtype=torch.float32, device=dev)
+    par = torch.empty((2 * Pp, Dp), dtype=torch.float32, device=dev)
+    freq = torch.empty((Pp, Dp // 2 + 1, 2), dtype=torch.float32, device=dev)
+    img = torch.empty((N, N), dtype=torch.float32, device=dev)
+    names = ("attenuation", "fan2para", "filter_cufft", "backprojection", "mask")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+    acc = dict.fromkeys(names, 0.0)
+
+    def frame(f, timed):
+        k = f % L
+        steps = (lambda: rk.attenuation(raw[f], t_mask, fan, t_ref, t_dark, Df, Pf, k, 16),
+                 lambda: (par.zero_(), rk.fan2para_run(k, fan, par, f2p_in)),
+                 lambda: rk.filter_rows(par, freq, t_h, Dp, Pp, 16),
+                 lambda: rk.backproject(False, par, img, N, Pp, Dp, 16),
+                 lambda: rk.mask(img, 0.0, N))
+        ev[0].record(stream)
+        for i, step in enumerate(steps):
+            step()
+            ev[i + 1].record(stream)
+            stream.synchronize()
+        if timed:
+            for i, nm in enumerate(names):
+                acc[nm] += ev[i].elapsed_time(ev[i + 1])
+
+    with torch.cuda.stream(stream):
+        for f in range(2):
+            frame(f, False)
+        t0 = time.perf_counter()
+        for f in range(n_frames):
+            frame(f, True)
+        wall = time.perf_counter() - t0
+    ms = {k: v / n_frames for k, v in acc.items()}
+    return {"value": n_frames / wall, "unit": "slices/s", "frames": n_frames,
+            "kernel_ms_per_slice": ms, "bp_gupdates_per_s": N * N * Pp / (ms["backprojection"] / 1e3) / 1e9,
+            "filter_length": Dp,
+            "how": "the reference's own stage kernels (cubins built from its sources for sm_103a), one frame per "
+                   "stage launch, 16x16 blocks, stream sync after each stage; RISA quirks; unpadded filter of "
+                   f"length {Dp} (this library: {2 * Dp}); no defect repair (host-side in the reference)"}
 
 
 def cuda_ms(torch, fn, reps=5):

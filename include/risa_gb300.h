@@ -163,11 +163,15 @@ risa_gb_status risa_gb_defects_destroy(risa_gb_defects* h);
  * the scratch lives in a fixed 4 MiB device array inside the library, held on
  * every GPU that loads it until the process exits. Batches whose scratch would
  * exceed 4 MiB (about 180 frames of 1152 detectors per call) are rejected with
- * RISA_GB_EINVAL. The first call on a device sets up that device (it looks up
- * the array's address and uploads constants), so make it before any stream
- * capture. All calls share the array and it keeps the last call's contents;
- * calls whose GPU work overlaps race, so serialise them. Results are identical
- * to risa_gb_defects_enqueue with the same geometry and params. */
+ * RISA_GB_EINVAL. Every call looks up the array's address in the current CUDA
+ * context; the first call in a context (the first on a device, and the first
+ * after a cudaDeviceReset) also uploads the threshold constants, which
+ * synchronises the device, so make that call before any stream capture: if
+ * the set-up is due while `stream` is capturing, the call returns
+ * RISA_GB_EUNSUPPORTED and launches nothing. All calls share the array and it
+ * keeps the last call's contents; calls whose GPU work overlaps race, so
+ * serialise them. Results are identical to risa_gb_defects_enqueue with the
+ * same geometry and params. */
 risa_gb_status risa_gb_defects_enqueue_noalloc(const risa_gb_geometry* g, const risa_gb_params* p,
                                                uint16_t* frames, int batch, int32_t* flags_out,
                                                void* stream);
@@ -447,6 +451,80 @@ risa_gb_status risa_gb_sweep_check(risa_gb_sweep* h);
 /* CTAs of the last persistent launch. */
 int risa_gb_sweep_grid(const risa_gb_sweep* h);
 risa_gb_status risa_gb_sweep_destroy(risa_gb_sweep* h);
+
+/* ---------------------------------------------------------------------------
+ * Online input: the detector modules' packets assembled into whole frames,
+ * replacing the reference's per-module receivers and their notification
+ * (ReceiverModule.cpp:56-116, OnlineReceiverNotification.h:53-79,
+ * Receiver.cpp:71-86); sockets stay with the caller, which passes each packet
+ * it receives. A packet is [uint64 frame index][uint16 part]
+ * [proj_per_packet x det_per_module uint16] in native byte order. The ring is
+ * caller memory of ring x modules x proj x det_per_module uint16: whole frames
+ * in the module-major order that risa_gb_params.module_major reads, so a
+ * frame goes to the device in one copy (pinned host memory) with no
+ * reordering pass. Completion rules:
+ *   RISA_GB_COMPLETION_EXACT      every part of every module arrived; frames
+ *                                 handed out in index order; an incomplete
+ *                                 frame is given up once a frame skip_lag
+ *                                 newer is complete (0: half the ring)
+ *   RISA_GB_COMPLETION_LAST_PART  the reference's rule: a module announces a
+ *                                 frame with its last part, the newest frame
+ *                                 every module announced is handed out if it
+ *                                 is newer than the last (frame 0 never is);
+ *                                 parts lost earlier keep the slot's old data
+ * A slot is reused only after release() (or once its frame was passed over);
+ * until then a packet for it gets RISA_GB_INGEST_RING_FULL and the sender
+ * retries. */
+typedef struct risa_gb_packet_layout {
+   uint32_t struct_size;    /* sizeof(risa_gb_packet_layout) */
+   int32_t modules;         /* numberOfDetectorModules */
+   int32_t det_per_module;  /* numberOfDetectorsPerModule */
+   int32_t proj;            /* projections per frame */
+   int32_t proj_per_packet; /* numberOfProjectionsPerPacket (divides proj) */
+   int32_t ring;            /* inputBufferSize: frames in the ring */
+} risa_gb_packet_layout;
+#define RISA_GB_COMPLETION_EXACT 0
+#define RISA_GB_COMPLETION_LAST_PART 1
+#define RISA_GB_INGEST_ACCEPTED 0
+#define RISA_GB_INGEST_DUPLICATE 1
+#define RISA_GB_INGEST_MALFORMED 2
+#define RISA_GB_INGEST_STALE 3
+#define RISA_GB_INGEST_RING_FULL 4
+typedef struct risa_gb_assembler risa_gb_assembler;
+risa_gb_status risa_gb_assembler_create(const risa_gb_packet_layout* layout, uint16_t* ring, int skip_lag,
+                                        int completion, risa_gb_assembler** out);
+/* One packet of module `module`; thread-safe (one thread per module may call
+ * it concurrently with the consumer). Returns a RISA_GB_INGEST_* outcome
+ * (>= 0), or RISA_GB_EINVAL for a null handle. */
+int risa_gb_assembler_ingest(risa_gb_assembler* h, int module, const void* packet, size_t bytes);
+/* Waits up to timeout_s for the next frame: 1 with its index and ring slot
+ * (frame memory = ring + slot * modules * proj * det_per_module), 0 on
+ * timeout or once finish() was called and nothing is left; < 0 on error. */
+int risa_gb_assembler_next(risa_gb_assembler* h, double timeout_s, uint64_t* index, int* slot);
+/* The consumer is done with frame `index`: its slot may be reused. */
+risa_gb_status risa_gb_assembler_release(risa_gb_assembler* h, uint64_t index);
+/* No more packets: next() drains what can still be handed out, then returns 0. */
+risa_gb_status risa_gb_assembler_finish(risa_gb_assembler* h);
+/* Frames skipped (never handed out), incomplete slots taken over, duplicate
+ * packets. Any pointer may be NULL. */
+risa_gb_status risa_gb_assembler_stats(risa_gb_assembler* h, uint64_t* skipped, uint64_t* abandoned,
+                                       uint64_t* duplicates);
+risa_gb_status risa_gb_assembler_destroy(risa_gb_assembler* h);
+
+/* ---------------------------------------------------------------------------
+ * Measured on-chip peaks (no counterpart in the reference: a measurement
+ * utility). The backprojection is bound by shared-memory reads and its
+ * arithmetic is FP32; these micro-benchmarks give the roofline denominators
+ * on the GPU they run on. kind RISA_GB_PEAK_SMEM_READ: 128-bit conflict-free
+ * shared-memory loads, 2 CTAs of 512 threads per SM; RISA_GB_PEAK_FP32_FMA:
+ * independent fma.rn.f32 chains, 4 CTAs of 256 threads per SM. Best of `reps`
+ * launches (CUDA events on `stream`, after one warm-up). out[4]: rate (GB/s or
+ * TFLOP/s), rate per SM per clock (bytes or FLOP), the mean SM clock during
+ * that launch (MHz, from clock64 against %globaltimer), SM count.
+ * Allocates and synchronises: not for the hot path. */
+#define RISA_GB_PEAK_SMEM_READ 0
+#define RISA_GB_PEAK_FP32_FMA 1
+risa_gb_status risa_gb_measure_peak(int kind, int reps, void* stream, double* out);
 
 #ifdef __cplusplus
 }

@@ -28,6 +28,17 @@ BP_LINEAR, BP_NEAREST, BP_NEAREST_TRUNC = 0, 1, 2
 MAX_PLANES = 4
 
 
+def reference_root() -> str:
+    """Where the reference checkout is looked for by the reference-side harness
+    (oracle/ref_harness): RISA_REF_ROOT if set, else the path written in
+    oracle/ref_harness/reference_root, the one place that names it."""
+    env = os.environ.get("RISA_REF_ROOT")
+    if env:
+        return env
+    with open(os.path.join(HERE, "ref_harness", "reference_root")) as f:
+        return f.readline().strip()
+
+
 def build(force: bool = False) -> str:
     """Compile risa_oracle.c into oracle/_build/librisa_oracle.so (gcc, no FMA contraction)."""
     src = os.path.join(HERE, "risa_oracle.c")

@@ -1,17 +1,18 @@
 #!/usr/bin/env bash
 # Builds the reference-side test harnesses from the read-only reference tree,
-# in place, with outputs only under oracle/_ref/. Needs the reference checkout
-# (RISA_REF_ROOT, default /root/reference); prints a note and exits 0 without it.
+# in place, with outputs only under oracle/_ref/. Needs the reference checkout:
+# RISA_REF_ROOT if set, else the path in oracle/ref_harness/reference_root (the
+# one place that names it); prints where it looked and exits 0 without it.
 #   librisa_ref_host.so : the reference's host-side table builders (CPU only)
 #   risa_*.cubin        : the reference's stage kernels for sm_103a (device code
 #                         only; they travel to the GPU host, where
 #                         build_launch.sh builds the launcher that runs them)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${RISA_REF_ROOT:-/root/reference}"
+REF="${RISA_REF_ROOT:-$(head -n1 "$HERE/reference_root")}"
 OUT="$HERE/../_ref"
 if [ ! -d "$REF/RISA/risaLib/src" ]; then
-  echo "build_ref: reference tree not found at $REF; skipping"; exit 0
+  echo "build_ref: no reference tree at '$REF' (set RISA_REF_ROOT or edit oracle/ref_harness/reference_root); skipping"; exit 0
 fi
 mkdir -p "$OUT"
 NVCC="${NVCC:-nvcc}"

@@ -58,6 +58,72 @@ def lib() -> ctypes.CDLL:
     return _lib
 
 
+def bp_setup(n_proj: int, n_det: int, n_pixels: int, rotation_offset: float = 0.0):
+    """The host set-up of Backprojection::processor (Backprojection.cu:118-138):
+    (sin table, cos table, norm, scale, center) with the reference's float steps."""
+    import numpy as np
+
+    sin_t = np.zeros(n_proj, np.float32)
+    cos_t = np.zeros(n_proj, np.float32)
+    for i in range(n_proj):
+        th = np.float32(i * np.pi / float(np.float32(n_proj)) + float(np.float32(rotation_offset)) / 180.0 * np.pi)
+        while th < 0.0:
+            th = np.float32(float(th) + 2.0 * np.pi)
+        sin_t[i] = np.float32(np.sin(np.float64(th)))
+        cos_t[i] = np.float32(np.cos(np.float64(th)))
+    scale = np.float32(n_det / float(np.float32(n_pixels)))
+    norm = np.float32(np.pi / n_proj / float(scale))
+    center = np.float32((n_pixels - 1.0) * 0.5)
+    return sin_t, cos_t, float(norm), float(scale), float(center)
+
+
+def fan2para_inputs(geom: dict, z: dict, block: int = 16) -> dict:
+    """Device inputs of the reference's interpolation kernel for a geometry and its
+    reference-layout tables z (theta, gamma, s, alpha, itab[10], ftab[4], as the
+    reference's computeFan2ParaTransp writes them). The kernel reads the tables
+    without bounds checks and its own bounds test lets threads past the edge
+    run unless the grid covers the sinogram exactly, so both are checked here
+    on the CPU before anything reaches the GPU."""
+    import numpy as np
+    import torch
+
+    L, Pf, Df = geom["n_planes"], geom["n_fan_proj"], geom["n_fan_det"]
+    Pp2, Dp = 2 * geom["n_par_proj"], geom["n_par_det"]
+    itab, ftab = z["itab"], z["ftab"]
+    if itab.shape != (10, L * Pp2 * Dp) or ftab.shape != (4, L * Pp2 * Dp):
+        raise ValueError("fan2para tables do not match the geometry")
+    if Dp % block or Pp2 % block:
+        raise ValueError("the reference kernel's grid must cover the sinogram exactly")
+    if not (len(z["gamma"]) == Df and len(z["theta"]) == Pf and len(z["s"]) == Dp and len(z["alpha"]) == Pp2):
+        raise ValueError("fan2para axis tables do not match the geometry")
+    for r in (0, 1):
+        on = itab[8 + r] != 0
+        for row, lim in ((0 + r, Pf), (2 + r, Pf), (4 + r, Df), (6 + r, Df)):
+            v = itab[row][on]
+            if v.size and (v.min() < 0 or v.max() >= lim):
+                raise ValueError("fan2para table index out of range")
+
+    def dev(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+    order = [itab[0], itab[1], itab[2], itab[3], itab[6], itab[7], itab[4], itab[5],
+             ftab[0], ftab[1], ftab[2], ftab[3], itab[8], itab[9]]
+    params = np.zeros(11, np.int32)
+    params[:5] = (L, Df, Pf, Pp2, Dp)
+    params[5:].view(np.float32)[:] = (geom["source_offset"], geom["detector_diameter"],
+                                      geom["detector_diameter"] / 2.0, geom.get("image_center_x", 0.0),
+                                      geom.get("image_center_y", 0.0), geom["image_width"])
+    return dict(tables=[dev(t) for t in order], params=dev(params), gamma=dev(z["gamma"]), theta=dev(z["theta"]),
+                alpha=dev(z["alpha"]), s=dev(z["s"]), n_par_det=Dp, n_par_proj360=Pp2, block=block)
+
+
+def fan2para_run(plane: int, fan, par, inp: dict):
+    """One launch of the reference's interpolation kernel with fan2para_inputs();
+    par ([2 Pp][Dp] floats) must be zeroed first, as the reference's setValue does."""
+    fan2para(plane, fan, par, inp["gamma"], inp["theta"], inp["alpha"], inp["s"], inp["tables"], inp["params"],
+             inp["n_par_det"], inp["n_par_proj360"], inp["block"])
+
+
 def _ck(rc: int):
     if rc != 0:
         raise RuntimeError("reference kernels: " + lib().rr_error().decode())

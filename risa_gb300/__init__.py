@@ -149,6 +149,14 @@ SIGNATURES = {
     "risa_gb_sweep_times": (_i, [_vp, _vp, _vp, _vp]),
     "risa_gb_sweep_check": (_i, [_vp]),
     "risa_gb_sweep_grid": (_i, [_vp]),
+    "risa_gb_measure_peak": (_i, [_i, _i, _vp, ctypes.POINTER(ctypes.c_double)]),
+    "risa_gb_assembler_create": (_i, [_vp, _vp, _i, _i, _pp]),
+    "risa_gb_assembler_ingest": (_i, [_vp, _i, ctypes.c_char_p, _sz]),
+    "risa_gb_assembler_next": (_i, [_vp, _d, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]),
+    "risa_gb_assembler_release": (_i, [_vp, ctypes.c_uint64]),
+    "risa_gb_assembler_finish": (_i, [_vp]),
+    "risa_gb_assembler_stats": (_i, [_vp, _vp, _vp, _vp]),
+    "risa_gb_assembler_destroy": (_i, [_vp]),
     "risa_gb_sweep_destroy": (_i, [_vp]),
 }
 
@@ -620,6 +628,77 @@ class FBP(_Handle):
 
     def backprojection(self) -> Backprojection:
         return Backprojection(self.geom, self.params, handle=lib().risa_gb_fbp_backprojection(self._h))
+
+
+PEAK_SMEM_READ, PEAK_FP32_FMA = 0, 1
+COMPLETION_EXACT, COMPLETION_LAST_PART = 0, 1
+INGEST_ACCEPTED, INGEST_DUPLICATE, INGEST_MALFORMED, INGEST_STALE, INGEST_RING_FULL = range(5)
+
+
+class PacketLayout(ctypes.Structure):
+    """Mirror of risa_gb_packet_layout."""
+    _fields_ = [("struct_size", ctypes.c_uint32), ("modules", ctypes.c_int32), ("det_per_module", ctypes.c_int32),
+                ("proj", ctypes.c_int32), ("proj_per_packet", ctypes.c_int32), ("ring", ctypes.c_int32)]
+
+
+def packet_layout(modules: int, det_per_module: int, proj: int, proj_per_packet: int, ring: int) -> PacketLayout:
+    return PacketLayout(ctypes.sizeof(PacketLayout), modules, det_per_module, proj, proj_per_packet, ring)
+
+
+def encode_packet(index: int, part: int, payload) -> bytes:
+    """[uint64 frame index][uint16 part][payload uint16] in native byte order."""
+    import struct
+
+    return struct.pack("=QH", index, part) + payload.tobytes()
+
+
+class Assembler(_Handle):
+    """Online input: module packets -> whole module-major frames in a caller ring
+    (risa_gb_assembler_*). `ring` is a uint16/int16 buffer of layout.ring frames
+    that outlives this object (pinned host memory for one-copy uploads)."""
+    _destroy = "risa_gb_assembler_destroy"
+
+    def __init__(self, layout: PacketLayout, ring, skip_lag: int = 0, completion: int = COMPLETION_EXACT):
+        super().__init__()
+        self.layout, self.ring = layout, ring
+        _check(lib().risa_gb_assembler_create(ctypes.byref(layout), ptr(ring), skip_lag, completion,
+                                              ctypes.byref(self._h)), "assembler_create")
+
+    def ingest(self, module: int, packet: bytes) -> int:
+        r = lib().risa_gb_assembler_ingest(self._h, module, packet, len(packet))
+        if r < 0:
+            raise RisaError(r, "assembler_ingest", last_error())
+        return r
+
+    def next(self, timeout_s: float):
+        """(frame index, ring slot), or None on timeout / when finished and drained."""
+        idx, slot = ctypes.c_uint64(), ctypes.c_int()
+        r = lib().risa_gb_assembler_next(self._h, timeout_s, ctypes.byref(idx), ctypes.byref(slot))
+        if r < 0:
+            raise RisaError(r, "assembler_next", last_error())
+        return (idx.value, slot.value) if r == 1 else None
+
+    def release(self, index: int):
+        _check(lib().risa_gb_assembler_release(self._h, index), "assembler_release")
+
+    def finish(self):
+        _check(lib().risa_gb_assembler_finish(self._h), "assembler_finish")
+
+    def stats(self) -> dict:
+        v = [ctypes.c_uint64() for _ in range(3)]
+        _check(lib().risa_gb_assembler_stats(self._h, *[ctypes.byref(x) for x in v]), "assembler_stats")
+        return dict(zip(("skipped", "abandoned", "duplicates"), (x.value for x in v)))
+
+
+def measure_peak(kind: int, reps: int = 5, stream=None) -> dict:
+    """Measured shared-memory read bandwidth (kind PEAK_SMEM_READ) or FP32 FMA
+    throughput (PEAK_FP32_FMA) of the current GPU; see risa_gb_measure_peak."""
+    out = (ctypes.c_double * 4)()
+    _check(lib().risa_gb_measure_peak(kind, reps, stream_ptr(stream), out), "measure_peak")
+    unit = "GB/s" if kind == PEAK_SMEM_READ else "TFLOP/s"
+    per = "B/clk/SM" if kind == PEAK_SMEM_READ else "FLOP/clk/SM"
+    return {"value": out[0], "unit": unit, "per_sm_per_clk": out[1], "per_sm_per_clk_unit": per,
+            "sm_mhz": out[2], "sms": int(out[3])}
 
 
 class Sweep(_Handle):

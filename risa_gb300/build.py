@@ -28,7 +28,7 @@ def _nvcc() -> str:
 
 def _headers():
     return (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
-            glob.glob(os.path.join(INCLUDE, "*.h")))
+            glob.glob(os.path.join(INCLUDE, "*.h")) + glob.glob(os.path.join(PKG, "cpp", "*", "*.h")))
 
 
 def _stale(obj: str, src: str) -> bool:

@@ -13,11 +13,21 @@
 //
 // Here packets land directly in a caller-owned ring of whole frames in that
 // module-major layout -- the layout the engine's module_major mode reads, so a
-// frame goes to the device with one copy and no reordering. Completion is
-// exact: a frame is complete when every part of every module has arrived
-// (a lost packet is detected, not overwritten silently). Frames are handed out
-// in index order; an incomplete frame older than a complete one is skipped and
-// counted, as the reference's newest-common-frame rule skips it. Sockets are
+// frame goes to the device with one copy and no reordering. Two completion
+// rules (Completion):
+//   exact (default): a frame is complete when every part of every module has
+//     arrived (a lost packet is detected, not overwritten silently); frames are
+//     handed out in index order, and an incomplete frame is given up once a
+//     frame skip_lag newer is complete (counted as skipped);
+//   last_part: the reference's rule -- a module announces a frame when the
+//     frame's last part arrives (ReceiverModule.cpp:85-86,111-112) and the
+//     frame handed out is the newest one every module has announced, provided
+//     it is newer than the last one handed out (OnlineReceiverNotification.h:
+//     53-79, whose last index starts at 0, so frame 0 is never handed out).
+//     Parts lost before the last one leave what the slot held before, and the
+//     frames between two hand-outs are skipped.
+// Unlike the reference's receiver, a slot whose frame has not been released
+// is never overwritten (the sender gets ring_full and retries). Sockets are
 // not part of this file: any transport calls ingest() with the packet bytes.
 #pragma once
 #include <algorithm>
@@ -61,6 +71,9 @@ inline void encode_packet(const PacketLayout& L, uint64_t index, uint16_t part, 
 // Outcome of FrameAssembler::ingest.
 enum class Ingest { accepted, duplicate, malformed, stale, ring_full };
 
+// When a frame may be handed out (see the top of this file).
+enum class Completion { exact, last_part };
+
 // Assembles packets of all modules into whole frames in a ring of layout.ring
 // frames [ring][module][projection][detector] (caller-owned, e.g. pinned host
 // memory). Thread-safe: one thread per module may call ingest() concurrently
@@ -68,16 +81,26 @@ enum class Ingest { accepted, duplicate, malformed, stale, ring_full };
 // the lock, so a slot is never reused while a packet is being written to it.
 class FrameAssembler {
   public:
-   // skip_lag: an incomplete frame is given up once a frame that many indices
-   // newer is complete (default: half the ring; must be below the ring size so
-   // that frame has a slot of its own)
-   FrameAssembler(const PacketLayout& layout, uint16_t* frames, int skip_lag = 0)
+   // skip_lag (exact rule): an incomplete frame is given up once a frame that
+   // many indices newer is complete (default: half the ring; must be below the
+   // ring size so that frame has a slot of its own)
+   FrameAssembler(const PacketLayout& layout, uint16_t* frames, int skip_lag = 0,
+                  Completion rule = Completion::exact)
        : L_(layout), frames_(frames), slots_(layout.ring),
-         lag_(skip_lag > 0 ? skip_lag : (layout.ring / 2 > 0 ? layout.ring / 2 : 1)) {
+         lag_(skip_lag > 0 ? skip_lag : (layout.ring / 2 > 0 ? layout.ring / 2 : 1)), rule_(rule) {
       if (!L_.valid() || !frames_ || lag_ >= std::max(2, L_.ring))
          throw std::invalid_argument("FrameAssembler: inconsistent packet layout or skip lag");
       for (auto& s : slots_) s.have.assign((size_t)L_.modules * L_.parts(), 0);
+      if (rule_ == Completion::last_part) {
+         // the reference's notification starts with every module at index 0
+         // and its last handed-out index at 0
+         announced_.assign(L_.modules, 0);
+         delivered_any_ = true;
+         last_delivered_ = 0;
+      }
    }
+
+   Completion rule() const { return rule_; }
 
    const PacketLayout& layout() const { return L_; }
 
@@ -95,9 +118,10 @@ class FrameAssembler {
       if (!s.used || s.index != index) {
          if (s.used && index < s.index) return Ingest::stale;
          // The slot's frame is taken over only once the consumer released it,
-         // or -- incomplete -- once a newer frame was delivered past it (it was
-         // skipped). Otherwise the sender is ahead by a whole ring: it retries.
-         const bool skipped = s.used && !s.complete && delivered_any_ && s.index < last_delivered_;
+         // or -- never handed out -- once a newer frame was delivered past it
+         // (it was skipped). Otherwise the sender is ahead by a whole ring: it
+         // retries.
+         const bool skipped = s.used && !s.delivered && delivered_any_ && s.index < last_delivered_;
          if (s.used && !s.released && !skipped) return Ingest::ring_full;
          if (skipped) ++abandoned_;
          s.used = true;
@@ -117,6 +141,10 @@ class FrameAssembler {
       s.have[bit] = 1;
       if (++s.count == L_.modules * L_.parts()) {
          s.complete = true;
+         if (rule_ == Completion::exact) cv_.notify_all();
+      }
+      if (rule_ == Completion::last_part && (int)part == L_.parts() - 1) {
+         if (announced_[module] < index) announced_[module] = index;
          cv_.notify_all();
       }
       return Ingest::accepted;
@@ -128,6 +156,7 @@ class FrameAssembler {
    bool next(uint64_t* index, const uint16_t** frame, double timeout_s) {
       std::unique_lock<std::mutex> lk(m_);
       const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+      if (rule_ == Completion::last_part) return next_last_part(lk, deadline, index, frame);
       for (;;) {
          Slot* best = nullptr;
          uint64_t newest_complete = 0;
@@ -183,6 +212,31 @@ class FrameAssembler {
    uint64_t duplicates() const { std::lock_guard<std::mutex> lk(m_); return duplicates_; }
 
   private:
+   // The reference's fetch(): the smallest of the modules' newest announced
+   // indices, once it exceeds the last index handed out.
+   template <class Deadline>
+   bool next_last_part(std::unique_lock<std::mutex>& lk, const Deadline& deadline, uint64_t* index,
+                       const uint16_t** frame) {
+      for (;;) {
+         const uint64_t m = *std::min_element(announced_.begin(), announced_.end());
+         if (m > last_delivered_) {
+            Slot& s = slots_[(size_t)(m % (uint64_t)L_.ring)];
+            skipped_ += m - last_delivered_ - 1;
+            last_delivered_ = m;
+            if (s.used && s.index == m) {  // always so: an unreleased slot is never taken over
+               s.delivered = true;
+               *index = m;
+               *frame = frames_ + (size_t)(&s - slots_.data()) * L_.frame_values();
+               return true;
+            }
+            ++skipped_;
+            continue;
+         }
+         if (finished_) return false;
+         if (cv_.wait_until(lk, deadline) == std::cv_status::timeout) return false;
+      }
+   }
+
    struct Slot {
       bool used = false, complete = false, delivered = false, released = false;
       uint64_t index = 0;
@@ -193,6 +247,8 @@ class FrameAssembler {
    uint16_t* frames_;
    std::vector<Slot> slots_;
    int lag_;
+   Completion rule_;
+   std::vector<uint64_t> announced_;  // last_part rule: newest announced index per module
    mutable std::mutex m_;
    std::condition_variable cv_;
    bool delivered_any_ = false, finished_ = false;

@@ -17,6 +17,18 @@
 // reading them. Calls whose GPU work overlaps (on different streams, or from
 // different host threads) race on the array and must be serialised by the
 // caller.
+//
+// Set-up. Host code cannot use the array's name as a device address, so every
+// call looks the address up with cudaGetSymbolAddress in the current context.
+// The threshold weights (a __constant__ table) and the shared-memory limit of
+// the flagging kernel belong to a context too: they are uploaded on the first
+// call in each CUDA context, recognised by the driver's context ID, so a
+// cudaDeviceReset (after which the runtime builds a new context) or a switch
+// to another context is followed by a fresh upload. That upload synchronises
+// the legacy default stream, so it is refused while the caller's stream is
+// being captured into a graph.
+#include <cuda.h>
+
 #include <mutex>
 #include <string>
 
@@ -33,28 +45,68 @@ __device__ __align__(256) unsigned char g_defect_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-void* g_scratch_ptr[kMaxDevices] = {nullptr};
+unsigned long long g_setup_ctx[kMaxDevices] = {0};  // context ID whose set-up is done (0: none)
 
-// Device address of the array for the current device. The first call on a
-// device looks it up (with that device current) and uploads the threshold
-// weights; this set-up should happen before any stream capture.
-risa_gb_status scratch_for_current_device(void** out) {
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+std::once_flag g_driver_once;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// ID of the current context (unique for the life of the process), through the
+// driver entry points the runtime hands out, so the library needs no libcuda
+// link of its own.
+risa_gb_status current_context_id(unsigned long long* id) {
+   std::call_once(g_driver_once, [] {
+      void* fn = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) ==
+              cudaSuccess && q == cudaDriverEntryPointSuccess)
+         g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+      fn = nullptr;
+      if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+          q == cudaDriverEntryPointSuccess)
+         g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(fn);
+   });
+   if (!g_ctx_get_current || !g_ctx_get_id)
+      return fail(RISA_GB_ECUDA, "the driver does not provide cuCtxGetCurrent/cuCtxGetId");
+   CUcontext ctx = nullptr;
+   if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return fail(RISA_GB_ECUDA, "no current CUDA context");
+   if (g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return fail(RISA_GB_ECUDA, "cuCtxGetId failed");
+   return RISA_GB_OK;
+}
+
+// Device address of the array in the current context; uploads the constants
+// when this context has not been set up yet.
+risa_gb_status scratch_for_current_context(cudaStream_t stream, void** out) {
    int dev = 0;
    cudaError_t e = cudaGetDevice(&dev);
    if (e != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
    if (dev < 0 || dev >= kMaxDevices) return fail(RISA_GB_EUNSUPPORTED, "device ordinal out of range");
+   void* p = nullptr;
+   e = cudaGetSymbolAddress(&p, g_defect_scratch);  // also makes the runtime's context current
+   if (e != cudaSuccess || !p)
+      return fail(RISA_GB_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+   unsigned long long ctx = 0;
+   risa_gb_status st = current_context_id(&ctx);
+   if (st) return st;
    std::lock_guard<std::mutex> lock(g_setup_mutex);
-   if (!g_scratch_ptr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_defect_scratch);
-      if (e != cudaSuccess || !p)
-         return fail(RISA_GB_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+   if (g_setup_ctx[dev] != ctx) {
+      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+      e = cudaStreamIsCapturing(stream, &cap);
+      if (e != cudaSuccess)
+         return fail(RISA_GB_ECUDA, std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+      if (cap != cudaStreamCaptureStatusNone)
+         return fail(RISA_GB_EUNSUPPORTED,
+                     "this CUDA context has not been set up for risa_gb_defects_enqueue_noalloc (first call "
+                     "on the device, or first call after a device reset) and the set-up cannot run while the "
+                     "stream is capturing: make one call outside the capture first");
       e = upload_defect_filter(0);
       if (e == cudaSuccess) e = cudaStreamSynchronize(0);
       if (e != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("defect set-up: ") + cudaGetErrorString(e));
-      g_scratch_ptr[dev] = p;
+      g_setup_ctx[dev] = ctx;
    }
-   *out = g_scratch_ptr[dev];
+   *out = p;
    return RISA_GB_OK;
 }
 
@@ -88,11 +140,11 @@ extern "C" risa_gb_status risa_gb_defects_enqueue_noalloc(const risa_gb_geometry
       return fail(RISA_GB_EINVAL, "batch too large for the fixed scratch: needs " + std::to_string(need) +
                                       " bytes, the limit is " + std::to_string(kScratchBytes));
    if (batch == 0) return RISA_GB_OK;
+   cudaStream_t s = static_cast<cudaStream_t>(stream);
    void* scratch = nullptr;
-   st = scratch_for_current_device(&scratch);
+   st = scratch_for_current_context(s, &scratch);
    if (st) return st;
    DefectWorkspace ws = defects_carve(scratch, cfg.D, batch, cfg.max_runs);
-   cudaStream_t s = static_cast<cudaStream_t>(stream);
    cudaError_t e = launch_defect_detect(frames, batch, cfg, ws, flags_out, s);
    if (e == cudaSuccess) e = launch_defect_repair(frames, batch, cfg, ws, s);
    if (e != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("defect kernels: ") + cudaGetErrorString(e));

@@ -150,6 +150,63 @@ int main() {
       EXPECT(fa.ingest(0, st.packet(L.ring, 0, 0), L.packet_bytes()) == Ingest::accepted);
    }
 
+   // 4. the reference's rule (Completion::last_part): a module announces a frame
+   //    with its last part; the newest frame all modules announced is handed
+   //    out; frame 0 never is; a lost middle part leaves the slot's old values;
+   //    frames between two hand-outs are skipped
+   {
+      std::vector<uint16_t> ring(L.ring * L.frame_values(), 0);
+      FrameAssembler fa(L, ring.data(), 0, Completion::last_part);
+      Stream st(L);
+      uint64_t idx;
+      const uint16_t* fr;
+      auto send = [&](uint64_t f, bool lose) {
+         for (int m = 0; m < L.modules; ++m)
+            for (int p = 0; p < L.parts(); ++p)
+               if (!(lose && m == 1 && p == 3)) {
+                  const Ingest r = fa.ingest(m, st.packet(f, m, p), L.packet_bytes());
+                  EXPECT(r == (f == 0 ? Ingest::stale : Ingest::accepted));
+               }
+      };
+      send(0, false);
+      EXPECT(!fa.next(&idx, &fr, 0.05));  // the reference's fetch never returns index 0
+      for (uint64_t f = 1; f < 10; ++f) {
+         // every module's last part but one: not yet announced by all
+         for (int m = 0; m < L.modules; ++m)
+            for (int p = 0; p < L.parts(); ++p)
+               if (!(f == 4 && m == 1 && p == 3) && !(m == L.modules - 1 && p == L.parts() - 1))
+                  EXPECT(fa.ingest(m, st.packet(f, m, p), L.packet_bytes()) == Ingest::accepted);
+         EXPECT(!fa.next(&idx, &fr, 0.01));
+         EXPECT(fa.ingest(L.modules - 1, st.packet(f, L.modules - 1, L.parts() - 1), L.packet_bytes()) ==
+                Ingest::accepted);
+         EXPECT(fa.next(&idx, &fr, 1.0) && idx == f);
+         if (f == 4) {
+            // slot 0 held nothing before (frame 0 was stale): the lost part reads 0
+            bool lost_zero = true, rest_ok = true;
+            for (int m = 0; m < L.modules; ++m)
+               for (int p = 0; p < L.proj; ++p)
+                  for (int d = 0; d < L.det_per_module; ++d) {
+                     const uint16_t v = fr[((size_t)m * L.proj + p) * L.det_per_module + d];
+                     if (m == 1 && p / L.proj_per_packet == 3) lost_zero &= v == 0;
+                     else rest_ok &= v == value(f, m, p, d);
+                  }
+            EXPECT(lost_zero && rest_ok);
+         } else {
+            EXPECT(frame_ok(L, f, fr));
+         }
+         fa.release(idx);
+      }
+      send(10, false);
+      send(11, false);
+      EXPECT(fa.next(&idx, &fr, 1.0) && idx == 11 && frame_ok(L, 11, fr));
+      EXPECT(fa.skipped() == 1);
+      fa.release(11);
+      fa.finish();
+      EXPECT(!fa.next(&idx, &fr, 1.0));
+      send(14, false);  // frame 10's slot (never handed out) is taken over
+      EXPECT(fa.abandoned() == 1);
+   }
+
    std::printf("packets: failures=%d\n", failures);
    return failures ? 1 : 0;
 }

@@ -26,6 +26,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "librisa_ref_host.so")
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
 
 # Geometries for the table fixtures. "rofex" is the reference's example
 # configuration (RISA/example/config.cfg:29-45) at reduced parallel sampling.
@@ -162,7 +164,9 @@ def make_filters(lib, out):
 
 
 def main():
-    if not os.path.isdir(os.environ.get("RISA_REF_ROOT", "/root/reference")):
+    import oracle
+
+    if not os.path.isdir(oracle.reference_root()):
         print("make_golden: the reference checkout is not available; nothing to do")
         return 0
     lib = load_ref()

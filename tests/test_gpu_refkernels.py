@@ -87,40 +87,31 @@ def test_attenuation_vs_reference_kernel(relevant):
 
 
 # ------------------------------------------------------------------------------ fan2para
-def test_fan2para_vs_reference_kernel(golden_dir):
-    gd = ROFEX_F2P
+# The full-rate streaming geometry in RISA mode: 2 planes, 1000 x 1152 fan
+# frames rebinned to 2048 x 1024 over 360 degrees (1024 x 1024 after the fold).
+CFG2_F2P = dict(n_planes=2, n_fan_det=1152, n_fan_proj=1000, n_par_proj=1024, n_par_det=1024, n_pixels=512,
+                source_offset=0.0, detector_diameter=480.0, image_center_x=0.0, image_center_y=0.0,
+                image_width=200.0, source_diameter=[430.0, 430.0], delta_x=[0.0, 0.0],
+                delta_z=[1417.0, 1430.0], source_angle=[360.0, 360.0])
+
+
+def _fan2para_case(gd, z):
+    """Library (RISA mode) vs the reference's interpolation kernel on the tables z
+    (the reference's host layout: theta, gamma, s, alpha, itab[10], ftab[4]);
+    fan2para_inputs checks the grid coverage and every table index on the CPU."""
     L, Pf, Df, Pp, Dp = gd["n_planes"], gd["n_fan_proj"], gd["n_fan_det"], gd["n_par_proj"], gd["n_par_det"]
     Pp2 = 2 * Pp
-    z = np.load(os.path.join(golden_dir, "f2p_rofex.npz"))
-    itab, ftab = z["itab"], z["ftab"]
-    # the reference kernel's bounds test lets threads past the detector edge run
-    # unless the grid covers the sinogram exactly; its table reads are unchecked
-    assert Dp % BLOCK == 0 and Pp2 % BLOCK == 0
-    for r in (0, 1):
-        on = itab[8 + r] != 0
-        for row, lim in ((0 + r, Pf), (2 + r, Pf), (4 + r, Df), (6 + r, Df)):
-            v = itab[row][on]
-            assert v.min() >= 0 and v.max() < lim
-    order = [itab[0], itab[1], itab[2], itab[3], itab[6], itab[7], itab[4], itab[5],
-             ftab[0], ftab[1], ftab[2], ftab[3], itab[8], itab[9]]
-    tables = [dev(t) for t in order]
-    params = np.zeros(11, np.int32)
-    params[:5] = (L, Df, Pf, Pp2, Dp)
-    params[5:].view(np.float32)[:] = (gd["source_offset"], gd["detector_diameter"],
-                                      gd["detector_diameter"] / 2.0, gd["image_center_x"],
-                                      gd["image_center_y"], gd["image_width"])
-    t_params = dev(params)
+    inp = rk.fan2para_inputs(gd, z, BLOCK)
     f2p = rg.Fan2Para(geom(gd), rg.make_params(quirks=rg.QUIRKS_RISA))
     rec = oracle.f2p_records(ns(gd), oracle.QUIRK_RISA)
     rng = np.random.default_rng(7)
     fan = rng.standard_normal((L, Pf, Df)).astype(np.float32)
     par = torch.empty((1, Pp, Dp), dtype=torch.float32, device="cuda")
-    t_g, t_t, t_a, t_s = dev(z["gamma"]), dev(z["theta"]), dev(z["alpha"]), dev(z["s"])
     for k in range(L):
         f2p.enqueue(dev(fan[k:k + 1]), par, k, 1)
         got = host(par)[0]
         ref_par = torch.zeros(Pp2 * Dp, dtype=torch.float32, device="cuda")
-        rk.fan2para(k, dev(fan[k]), ref_par, t_g, t_t, t_a, t_s, tables, t_params, Dp, Pp2, BLOCK)
+        rk.fan2para_run(k, dev(fan[k]), ref_par, inp)
         exp = host(ref_par)[:Pp * Dp].reshape(Pp, Dp)
         # The reference forms its interpolation weights with -use_fast_math
         # divisions (2 ulp), which moves its own output up to ~1e-5 (of the
@@ -131,6 +122,18 @@ def test_fan2para_vs_reference_kernel(golden_dir):
         print(f"plane {k}: lib vs FP64 {e_lib:.2e}, reference kernel vs FP64 {e_ref:.2e}, lib vs reference {e_pair:.2e}")
         assert e_lib < MAX_REL, (k, e_lib)
         assert e_pair < 2 * MAX_REL, (k, e_pair, e_ref)
+
+
+def test_fan2para_vs_reference_kernel(golden_dir):
+    """The reference's two-plane tilted ROFEX geometry, tables from the reference's host code."""
+    _fan2para_case(ROFEX_F2P, np.load(os.path.join(golden_dir, "f2p_rofex.npz")))
+
+
+def test_fan2para_vs_reference_kernel_full_rate_geometry():
+    """The full-rate streaming geometry; the reference-layout tables come from the
+    oracle's restatement of the reference's table builder, which the golden
+    vectors pin bit for bit (tests/test_oracle_golden.py)."""
+    _fan2para_case(CFG2_F2P, oracle.f2p_tables_risa(ns(CFG2_F2P)))
 
 
 # ------------------------------------------------------------------------------ filter
@@ -159,22 +162,6 @@ def test_filter_vs_reference_cufft_path(golden_dir, dp, ftype):
 
 
 # ------------------------------------------------------------------------------ backprojection
-def _bp_constants(Pp, Dp, N, rot):
-    """The host set-up of Backprojection::processor (Backprojection.cu:118-138)."""
-    sin_t = np.zeros(Pp, np.float32)
-    cos_t = np.zeros(Pp, np.float32)
-    for i in range(Pp):
-        th = np.float32(i * np.pi / float(np.float32(Pp)) + float(np.float32(rot)) / 180.0 * np.pi)
-        while th < 0.0:
-            th = np.float32(float(th) + 2.0 * np.pi)
-        sin_t[i] = np.float32(np.sin(np.float64(th)))
-        cos_t[i] = np.float32(np.cos(np.float64(th)))
-    scale = np.float32(Dp / float(np.float32(N)))
-    norm = np.float32(np.pi / Pp / float(scale))
-    center = np.float32((N - 1.0) * 0.5)
-    return sin_t, cos_t, float(norm), float(scale), float(center)
-
-
 @pytest.mark.parametrize("interp", [rg.INTERP_LINEAR, rg.INTERP_NEAREST])
 @pytest.mark.parametrize("Pp,Dp,N,rot", [(256, 256, 192, -7.5), (360, 512, 256, 0.0), (1024, 1024, 512, 0.0)])
 def test_backprojection_vs_reference_kernel(interp, Pp, Dp, N, rot):
@@ -183,7 +170,7 @@ def test_backprojection_vs_reference_kernel(interp, Pp, Dp, N, rot):
     bp = rg.Backprojection(g, p)
     bp.reserve(4)  # pair buffer, so the staged variants run as themselves
     sino, _ = phantom.parallel_sinograms(2, Pp, Dp, 200.0, seed=Pp)
-    sin_t, cos_t, norm, scale, center = _bp_constants(Pp, Dp, N, rot)
+    sin_t, cos_t, norm, scale, center = rk.bp_setup(Pp, Dp, N, rot)
     rk.bp_constants(sin_t, cos_t, Pp, norm, scale, center)
     img = torch.empty((2, N, N), dtype=torch.float32, device="cuda")
     ref_img = torch.empty((N, N), dtype=torch.float32, device="cuda")
