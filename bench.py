@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=512, help="frames per engine chunk (multiple of 2)")
     ap.add_argument("--distinct", type=int, default=8, help="distinct synthetic frames per plane")
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/roofline/cpu legs")
+    ap.add_argument("--scaling", choices=["weak", "strong"], default="weak",
+                    help="under torchrun: weak = every rank reconstructs the whole job; strong = the job's "
+                         "frames are split over the ranks (replicas.shard_indices) and the images gathered")
     ap.add_argument("--bp-variant", type=int, default=-1,
                     help="backprojection variant to use instead of autotuning (for profiling one kernel)")
     ap.add_argument("--only", choices=["precision", "differentiation", "sweep"], default=None,
@@ -196,7 +199,18 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     g = rg.make_geometry(**WORKLOAD)
     p = rg.make_params(filter_type="sheppLogan", defects=True, masking=True)
     sc = synthetic_scan(args.frames, args.distinct)
+    n_job = sc.raw.shape[0]
+    strong = args.scaling == "strong" and world > 1
+    if strong:  # this rank's plane groups of the job, dealt round robin
+        import dataclasses
+
+        from risa_gb300 import replicas
+
+        mine = replicas.shard_indices(n_job, rank, world, L)
+        sc = dataclasses.replace(sc, raw=np.ascontiguousarray(sc.raw[mine]), planes=sc.planes[mine])
     n = sc.raw.shape[0]
+    # frames all ranks reconstruct per step
+    job_frames = n_job if strong else world * n
     # a chunk never holds more frames than the job (every enqueue below reads B frames)
     B = min(args.batch, n)
     B -= B % L
@@ -248,33 +262,61 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * n / (ms / 1e3)
+    value = job_frames / (ms / 1e3)
     clocks = clk.summary()
 
+    gathered = None
+    if strong:
+        # every rank's images, reduced to one checksum per frame, collected on
+        # rank 0 in frame order; frames cycle through `distinct` source frames
+        # per plane, so equal sources must give equal checksums
+        from risa_gb300 import replicas
+
+        sums = img.double().sum(dim=(1, 2)).cpu().numpy()[:, None]
+        allsums = replicas.gather_images(sums, n_job, L)
+        if rank == 0:
+            period = args.distinct * L
+            gathered = {"frames": int(allsums.shape[0]),
+                        "frame_order_check": bool(np.array_equal(allsums[:, 0],
+                                                                 allsums[np.arange(n_job) % period, 0]))}
     extras = {}
+    if not args.no_extras:
+        # end to end through the host-buffer entry point, on every rank
+        t_e2e = measure_e2e(args, sc, fbp, torch, rg)
+        if world > 1:
+            t = torch.tensor([t_e2e], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        extras["e2e"] = {"value": job_frames / t_e2e, "unit": "slices/s",
+                         "h2d_bytes_per_step": int(job_frames * Pf * Df * 2),
+                         "d2h_bytes_per_step": int(job_frames * N * N * 4), "entry_point": "risa_gb_fbp_run_host"}
     if rank == 0 and not args.no_extras:
-        extras = measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
+        extras.update(measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p))
     if rank != 0:
         return
     peaks = measured_peaks()
     line = {
         "metric": "FBP slices/s @512^2", "value": value, "unit": "slices/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "scaling": "strong" if strong else "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded ellipse phantoms, Poisson uint16 counts; "
                 f"{args.distinct} distinct frames per plane cycled)",
-        "config": {"workload": WORKLOAD_NAME, "frames_per_plane": args.frames, "slices_per_step": n,
+        "config": {"workload": WORKLOAD_NAME, "frames_per_plane": args.frames, "slices_per_step": job_frames,
+                   "slices_per_rank": n,
                    "batch": B, "bp_variant": variant, "graph": "one CUDA graph per step",
                    "l2": "inputs larger than L2 (%.1f GB raw per step)" % (sc.raw.nbytes / 1e9),
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
     }
+    if gathered is not None:
+        line["gathered"] = gathered
     line.update(extras)
     if "plain" in line:
         line["speedup_vs_plain"] = value / world / line["plain"]["value"]
     if line.get("plain_reference", {}).get("value"):
         line["speedup_vs_plain_reference"] = value / world / line["plain_reference"]["value"]
+        line["e2e_speedup_vs_plain_reference"] = line["e2e"]["value"] / world / line["plain_reference"]["value"]
     if "roofline" in line and peaks:
         line["roofline"]["peaks_file"] = {k: peaks.get(k) for k in ("hbm_gbs", "sm_max_mhz")}
     print(json.dumps(line), flush=True)
@@ -292,6 +334,20 @@ def timed(torch, stream, fn, reps: int) -> float:
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1) / reps
+
+
+def measure_e2e(args, sc, fbp, torch, rg) -> float:
+    """Seconds per step through risa_gb_fbp_run_host: pinned host frames in,
+    pinned host images out, the copies inside the timed region."""
+    n, N = sc.raw.shape[0], WORKLOAD["n_pixels"]
+    hraw = torch.from_numpy(sc.raw.view(np.int16)).pin_memory()
+    himg = torch.empty((n, N, N), dtype=torch.float32).pin_memory()
+    fbp.run_host(hraw, himg, n, rg.PLANES_INTERLEAVED)  # warm-up (captures the slot graphs)
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        fbp.run_host(hraw, himg, n, rg.PLANES_INTERLEAVED)
+    return (time.perf_counter() - t0) / e2e_steps
 
 
 def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p):
@@ -411,18 +467,6 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     except Exception as e:  # reported, never hides the headline line
         out["plain_reference"] = {"error": f"{type(e).__name__}: {e}"}
     out["bp"]["reference_kernel"] = out["plain_reference"].get("bp_gupdates_per_s")
-
-    # ---- end to end through the host-buffer entry point
-    hraw = torch.from_numpy(sc.raw.view(np.int16)).pin_memory()
-    himg = torch.empty((n, N, N), dtype=torch.float32).pin_memory()
-    fbp.run_host(hraw, himg, n, rg.PLANES_INTERLEAVED)  # warm-up (captures the slot graphs)
-    e2e_steps = max(1, min(args.steps, 3))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        fbp.run_host(hraw, himg, n, rg.PLANES_INTERLEAVED)
-    t_e2e = (time.perf_counter() - t0) / e2e_steps
-    out["e2e"] = {"value": n / t_e2e, "unit": "slices/s", "h2d_bytes_per_step": int(sc.raw.nbytes),
-                  "d2h_bytes_per_step": int(n * N * N * 4), "entry_point": "risa_gb_fbp_run_host"}
 
     # ---- accuracy of the batched output against the FP64 oracle, and the CPU baseline
     cores = os.cpu_count() or 1

@@ -50,6 +50,18 @@ def gather_images(local: np.ndarray, n_frames: int, n_planes: int = 1, dst: int 
     return reassemble(parts, n_frames, world, n_planes) if rank == dst else None
 
 
+def run_sharded(n_frames: int, n_planes: int, reconstruct, dst: int = 0):
+    """One rank's part of a job split over the ranks (strong scaling): this
+    rank's frame indices (shard_indices), reconstructed by
+    `reconstruct(indices) -> images` -- the engine on this rank's GPU, or any
+    other worker -- then every rank's images collected on rank `dst` in frame
+    order. Returns the images there and None elsewhere."""
+    import torch.distributed as dist
+
+    idx = shard_indices(n_frames, dist.get_rank(), dist.get_world_size(), n_planes)
+    return gather_images(np.asarray(reconstruct(idx)), n_frames, n_planes, dst)
+
+
 def max_over_ranks(value: float) -> float:
     """The largest value over all ranks (e.g. the slowest rank's step time)."""
     import torch

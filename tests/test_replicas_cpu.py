@@ -1,7 +1,9 @@
 """Multi-GPU replicas, host side, on the CPU: the frame partition, reassembly in
-frame order, and a world_size-2 gloo run in which each rank reconstructs its
-share (the FP64 oracle stands in for the per-GPU engine) and rank 0 collects
-the images -- they must equal a single-process reconstruction of all frames."""
+frame order, and a world_size-2 gloo run of replicas.run_sharded -- the split
+a strong-scaling job takes -- in which each rank reconstructs the frame list
+it is given (the FP64 oracle stands in for the per-GPU engine) and rank 0
+collects the images: they must equal a single-process reconstruction of all
+frames, and each rank must have been given exactly its shard."""
 import os
 import socket
 
@@ -61,9 +63,14 @@ def _rank(rank, world, port, outdir):
     try:
         g, sc = _case()
         n = sc.raw.shape[0]
-        idx = replicas.shard_indices(n, rank, world, 2)
-        local = _oracle_fbp(g, sc, idx)
-        images = replicas.gather_images(local, n, n_planes=2)
+        given = []
+
+        def worker(idx):
+            given.append(np.asarray(idx))
+            return _oracle_fbp(g, sc, idx)
+
+        images = replicas.run_sharded(n, 2, worker)
+        np.save(os.path.join(outdir, f"given{rank}.npy"), given[0])
         slowest = replicas.max_over_ranks(1.5 + rank)
         if rank == 0:
             np.save(os.path.join(outdir, "gathered.npy"), images)
@@ -87,4 +94,7 @@ def test_two_gloo_ranks_match_one_process(tmp_path):
     expect = _oracle_fbp(g, sc, np.arange(sc.raw.shape[0]))
     got = np.load(tmp_path / "gathered.npy")
     np.testing.assert_array_equal(got, expect)
+    n = sc.raw.shape[0]
+    for r in range(world):
+        np.testing.assert_array_equal(np.load(tmp_path / f"given{r}.npy"), replicas.shard_indices(n, r, world, 2))
     assert float(np.load(tmp_path / "slowest.npy")[0]) == 2.5
