@@ -303,7 +303,9 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                 f"{args.distinct} distinct frames per plane cycled)",
         "config": {"workload": WORKLOAD_NAME, "frames_per_plane": args.frames, "slices_per_step": job_frames,
                    "slices_per_rank": n,
-                   "batch": B, "bp_variant": variant, "graph": "one CUDA graph per step",
+                   "batch": B, "bp_variant": variant,
+                   "graph": "one CUDA graph per step, two lanes (a chunk's backprojection beside the next "
+                            "chunk's streaming stages)",
                    "l2": "inputs larger than L2 (%.1f GB raw per step)" % (sc.raw.nbytes / 1e9),
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches_per_step * args.steps,
@@ -431,6 +433,17 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
         "defect_detect": {"ms": t_def, "gbs": B * fs * 2 / (t_def / 1e3) / 1e9},
         "hbm_peak_gbs": hbm, "batch": B,
     }
+
+    # ---- the same job as one lane: every stage of a chunk in sequence, no
+    # backprojection beside the next chunk's streaming stages
+    fbp.set_lanes(1)
+    g1 = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, stream)
+    ms1 = timed(torch, stream, lambda: g1.replay(stream), 2)
+    fbp.set_lanes(2)
+    out["one_lane"] = {"value": n / (ms1 / 1e3), "unit": "slices/s", "ms_per_step": ms1,
+                       "graph_kernels": g1.kernel_count,
+                       "how": "the headline's graph captured with risa_gb_fbp_set_lanes(1), CUDA events"}
+    del g1
 
     # ---- plain per-stage path: one frame per launch, sync after every stage
     dfx = rg.Defects(g, p, max_batch=1)

@@ -369,11 +369,15 @@ risa_gb_status risa_gb_fbp_create(const risa_gb_geometry* g, const risa_gb_param
 risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane,
                                    int batch, void* stream);
 /* Capture the reconstruction of n_frames device frames (any count: processed
- * in chunks of max_batch through the handle's buffers, chunk after chunk) as
- * one CUDA graph with fixed device pointers. Replaying it reruns the whole
- * job with a single launch. With interleaved planes, max_batch must be a
- * multiple of n_planes. The graph uses the handle's buffers: do not replay it
- * concurrently with other work on the same handle. */
+ * in chunks of max_batch through the handle's buffers) as one CUDA graph with
+ * fixed device pointers. Replaying it reruns the whole job with a single
+ * launch. With interleaved planes, max_batch must be a multiple of n_planes.
+ * With two lanes (risa_gb_fbp_set_lanes; the default) and more than one
+ * chunk, chunk c's backprojection runs beside chunk c+1's defect detection,
+ * attenuation, rebinning and filter, which run at the highest stream priority;
+ * the two lanes alternate between two pair-record buffers. The graph uses the
+ * handle's buffers: do not replay it concurrently with other work on the same
+ * handle, and capture again after a set-up call (reserve, autotune). */
 typedef struct risa_gb_graph risa_gb_graph;
 risa_gb_status risa_gb_fbp_graph_capture(risa_gb_fbp* h, const uint16_t* raw, float* img,
                                          int plane, int n_frames, void* stream,
@@ -385,10 +389,17 @@ risa_gb_status risa_gb_graph_destroy(risa_gb_graph* g);
 /* Host-buffer path, the H2D -> stages -> D2H flow of the reference's
  * H2D/D2H stages (H2D.cu:134-169, D2H.cu:119-148): copies n_frames raw
  * frames from host memory, reconstructs them in batches of the handle's
- * max_batch with copies overlapped against compute on two streams, and
+ * max_batch with copies overlapped against compute (and, with two lanes, one
+ * chunk's backprojection against the next chunk's streaming stages), and
  * copies the images back. Pinned host memory is fastest. Blocks until done. */
 risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, float* host_img,
                                     int n_frames, int plane);
+/* 2 (the default): chunks run as two lanes where the filter writes the
+ * backprojection's pair records (staged variants; otherwise one lane); 1:
+ * every stage of a chunk in sequence on one stream. Applies to later graph
+ * captures and host-path calls; results are identical either way. No
+ * reference counterpart (the reference runs one frame per stage call). */
+risa_gb_status risa_gb_fbp_set_lanes(risa_gb_fbp* h, int lanes);
 /* Per-stage access for inspection (intermediate device buffers). The engine
  * keeps attenuated fan frames as frame quads -- 4 frames of one plane side by
  * side, [quad][n_fan_proj][n_fan_det][4] float, quads of plane k before those of

@@ -150,6 +150,7 @@ SIGNATURES = {
     "risa_gb_sweep_check": (_i, [_vp]),
     "risa_gb_sweep_grid": (_i, [_vp]),
     "risa_gb_measure_peak": (_i, [_i, _i, _vp, ctypes.POINTER(ctypes.c_double)]),
+    "risa_gb_fbp_set_lanes": (_i, [_vp, _i]),
     "risa_gb_assembler_create": (_i, [_vp, _vp, _i, _i, _pp]),
     "risa_gb_assembler_ingest": (_i, [_vp, _i, ctypes.c_char_p, _sz]),
     "risa_gb_assembler_next": (_i, [_vp, _d, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]),
@@ -608,6 +609,11 @@ class FBP(_Handle):
         self._check_sizes(host_raw, host_img, n_frames, "fbp_run_host")
         _check(lib().risa_gb_fbp_run_host(self._h, ptr(host_raw), ptr(host_img), n_frames, plane),
                "fbp_run_host")
+
+    def set_lanes(self, lanes: int):
+        """2 (default): one chunk's backprojection beside the next chunk's
+        streaming stages in graphs and the host path; 1: stages in sequence."""
+        _check(lib().risa_gb_fbp_set_lanes(self._h, lanes), "fbp_set_lanes")
 
     def intermediates(self):
         fan, par = ctypes.c_void_p(), ctypes.c_void_p()

@@ -299,13 +299,24 @@ struct risa_gb_fbp {
    risa_gb_backprojection* bp = nullptr;
    risa_gb_masking* mask = nullptr;
    DevBuf fan, par, dws, mm;
+   // Two lanes (lanes = 2, where the filter writes the backprojection's pair
+   // records): chunk c's backprojection runs beside chunk c+1's streaming
+   // stages (defects, attenuation, rebinning, filter), which run at a higher
+   // stream priority; consecutive chunks alternate between two pair buffers.
+   // lanes = 1 runs every stage of a chunk in sequence.
+   int lanes = 2;
+   DevBuf pairs2;                  // the second pair buffer (the first is the backprojection's own)
+   cudaStream_t s_lane = nullptr;  // graph capture: the streaming-stage lane
+   cudaEvent_t ev_fork = nullptr, ev_pre = nullptr, ev_bpl[2] = {nullptr, nullptr};
    // host pipeline
    DevBuf raw_slot[2], img_slot[2];
-   cudaStream_t s_comp = nullptr, s_h2d = nullptr, s_d2h = nullptr;
+   cudaStream_t s_comp = nullptr, s_h2d = nullptr, s_d2h = nullptr, s_bp = nullptr;
    cudaEvent_t ev_h2d[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr},
-               ev_d2h[2] = {nullptr, nullptr};
-   cudaGraphExec_t slot_exec[2] = {nullptr, nullptr};
-   int slot_plane = 0x7fffffff;
+               ev_d2h[2] = {nullptr, nullptr}, ev_bp_slot[2] = {nullptr, nullptr};
+   cudaGraphExec_t slot_exec[2] = {nullptr, nullptr};      // one lane: the whole chunk
+   cudaGraphExec_t slot_bp_exec[2] = {nullptr, nullptr};   // two lanes: slot_exec = streaming stages
+   int slot_plane = 0x7fffffff, slot_lanes = 0;
+   const void* slot_pairs[2] = {nullptr, nullptr};  // pair buffers the slot graphs were captured with
 };
 
 // ============================================================================ C ABI
@@ -978,13 +989,20 @@ risa_gb_status risa_gb_fbp_destroy(risa_gb_fbp* h) {
    if (!h) return RISA_GB_OK;
    for (int i = 0; i < 2; ++i) {
       if (h->slot_exec[i]) cudaGraphExecDestroy(h->slot_exec[i]);
+      if (h->slot_bp_exec[i]) cudaGraphExecDestroy(h->slot_bp_exec[i]);
       if (h->ev_h2d[i]) cudaEventDestroy(h->ev_h2d[i]);
       if (h->ev_comp[i]) cudaEventDestroy(h->ev_comp[i]);
       if (h->ev_d2h[i]) cudaEventDestroy(h->ev_d2h[i]);
+      if (h->ev_bp_slot[i]) cudaEventDestroy(h->ev_bp_slot[i]);
+      if (h->ev_bpl[i]) cudaEventDestroy(h->ev_bpl[i]);
    }
+   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+   if (h->ev_pre) cudaEventDestroy(h->ev_pre);
+   if (h->s_lane) cudaStreamDestroy(h->s_lane);
    if (h->s_comp) cudaStreamDestroy(h->s_comp);
    if (h->s_h2d) cudaStreamDestroy(h->s_h2d);
    if (h->s_d2h) cudaStreamDestroy(h->s_d2h);
+   if (h->s_bp) cudaStreamDestroy(h->s_bp);
    risa_gb_defects_destroy(h->defects);
    risa_gb_attenuation_destroy(h->atten);
    risa_gb_fan2para_destroy(h->f2p);
@@ -1060,23 +1078,88 @@ static cudaError_t engine_filter_bp(risa_gb_fbp* h, float* par, float* img, int 
    return e;
 }
 
+// Defect detection, attenuation with the defect repair and the rebinning of
+// one chunk: raw frames -> parallel sinograms in h->par.
+static cudaError_t engine_streaming(risa_gb_fbp* h, const uint16_t* raw, int plane, int batch, cudaStream_t st) {
+   float* fan = h->fan.as<float>();
+   float* par = h->par.as<float>();
+   cudaError_t e;
+   if (h->defects) {
+      const DefectCfg& dc = h->defects->cfg;
+      DefectWorkspace ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs, true);
+      e = launch_defect_detect(raw, batch, dc, ws, nullptr, st);
+      if (e == cudaSuccess)
+         e = launch_attenuation_quads(raw, fan, batch, engine_atten_cfg(h, plane), &ws, dc.max_runs, st);
+   } else {
+      e = launch_attenuation_quads(raw, fan, batch, engine_atten_cfg(h, plane), nullptr, 0, st);
+   }
+   if (e == cudaSuccess) e = launch_fan2para_quads(fan, par, batch, h->f2p->cfg(plane), st);
+   return e;
+}
+
+// Whether chunks of `batch` frames run as two lanes: the filter writes the
+// backprojection's pair records (staged variant, radix-16 filter length), so
+// a chunk's backprojection reads nothing the next chunk's streaming stages
+// write but its own pair buffer.
+static bool two_lanes(const risa_gb_fbp* h, int batch) {
+   if (h->lanes < 2 || h->p.normalize || h->p.interp != RISA_GB_INTERP_LINEAR) return false;
+   const bool fused = h->p.masking && !h->p.normalize;
+   return bp_variant_pair_slices(h->bp->variant_for(batch, fused)) > 0 && filter_pairs_supported(h->filt->cfg());
+}
+
+// The second pair buffer, the capture lane (highest stream priority) and its
+// events. Set-up: may allocate and synchronise, never inside a capture.
+static risa_gb_status ensure_lanes(risa_gb_fbp* h) {
+   if (h->pairs2.bytes < h->bp->pairs.bytes) {
+      RG_CUDA(cudaDeviceSynchronize());
+      RG_TRY(h->pairs2.alloc(h->bp->pairs.bytes));
+   }
+   if (!h->s_lane) {
+      int least = 0, greatest = 0;
+      RG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      RG_CUDA(cudaStreamCreateWithPriority(&h->s_lane, cudaStreamNonBlocking, greatest));
+      RG_CUDA(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+      RG_CUDA(cudaEventCreateWithFlags(&h->ev_pre, cudaEventDisableTiming));
+      for (int i = 0; i < 2; ++i) RG_CUDA(cudaEventCreateWithFlags(&h->ev_bpl[i], cudaEventDisableTiming));
+   }
+   return RISA_GB_OK;
+}
+
+// Pair buffer i of the two lanes (0: the backprojection's own, 1: pairs2).
+static void* lane_pairs(risa_gb_fbp* h, int i) { return i ? h->pairs2.p : h->bp->pairs.p; }
+
+// The streaming lane's share of a chunk: the streaming stages, then the
+// filter writing the pair records into `pairs`.
+static cudaError_t engine_lane_prefix(risa_gb_fbp* h, const uint16_t* raw, int plane, int batch, void* pairs,
+                                      cudaStream_t st) {
+   cudaError_t e = engine_streaming(h, raw, plane, batch, st);
+   if (e != cudaSuccess) return e;
+   const bool fused = h->p.masking && !h->p.normalize;
+   const int v = h->bp->variant_for(batch, fused);
+   const BPCfg c = h->bp->cfg(fused);
+   return launch_filter_pairs(h->par.as<float>(), batch, h->filt->cfg(),
+                              PairsOut{pairs, bp_variant_pair_slices(v), c.win_lo, c.win_len}, st);
+}
+
+// The backprojection lane's share: the backprojection from `pairs` (both
+// pair buffers hold at least the backprojection's reservation).
+static cudaError_t engine_lane_bp(risa_gb_fbp* h, float* img, int batch, void* pairs, cudaStream_t st) {
+   const bool fused = h->p.masking && !h->p.normalize;
+   const int v = h->bp->variant_for(batch, fused);
+   BPCfg c = h->bp->cfg(fused);
+   c.pairs = pairs;
+   c.prefilled = true;
+   return launch_backprojection(h->par.as<float>(), img, batch, c, v, st);
+}
+
 risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* img, int plane, int batch,
                                    void* stream) {
    if (!h || !raw || !img) return fail(RISA_GB_EINVAL, "null handle or buffer");
    if (batch < 0 || batch > h->max_batch) return fail(RISA_GB_EINVAL, "batch exceeds max_batch");
    RG_TRY(check_plane(h->g, plane));
    cudaStream_t st = S(stream);
-   float* fan = h->fan.as<float>();
    float* par = h->par.as<float>();
-   if (h->defects) {
-      const DefectCfg& dc = h->defects->cfg;
-      DefectWorkspace ws = defects_carve(h->dws.p, dc.D, batch, dc.max_runs, true);
-      RG_CUDA(launch_defect_detect(raw, batch, dc, ws, nullptr, st));
-      RG_CUDA(launch_attenuation_quads(raw, fan, batch, engine_atten_cfg(h, plane), &ws, dc.max_runs, st));
-   } else {
-      RG_CUDA(launch_attenuation_quads(raw, fan, batch, engine_atten_cfg(h, plane), nullptr, 0, st));
-   }
-   RG_CUDA(launch_fan2para_quads(fan, par, batch, h->f2p->cfg(plane), st));
+   RG_CUDA(engine_streaming(h, raw, plane, batch, st));
    const bool fused = h->p.masking && !h->p.normalize;
    RG_CUDA(engine_filter_bp(h, par, img, batch, fused, st, nullptr, nullptr));
    if (h->p.normalize)
@@ -1138,12 +1221,47 @@ static risa_gb_status capture(risa_gb_fbp* h, const uint16_t* raw, float* img, i
    const int B = h->max_batch;
    if (plane == RISA_GB_PLANES_INTERLEAVED && n_frames > B && B % g.L != 0)
       return fail(RISA_GB_EINVAL, "interleaved planes need max_batch to be a multiple of n_planes");
+   // two lanes where the job has more than one chunk and every chunk size qualifies
+   bool lanes2 = n_frames > B && two_lanes(h, B);
+   for (int first = 0; lanes2 && first < n_frames; first += B) lanes2 = two_lanes(h, std::min(B, n_frames - first));
+   if (lanes2) RG_TRY(ensure_lanes(h));
    cudaGraph_t graph = nullptr;
+   std::vector<cudaGraphNode_t> bp_nodes;  // the backprojection lane's kernels (low priority)
    RG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
    risa_gb_status s = RISA_GB_OK;
-   for (int first = 0; first < n_frames && s == RISA_GB_OK; first += B) {
-      const int nb = std::min(B, n_frames - first);
-      s = risa_gb_fbp_enqueue(h, raw + (size_t)first * fs, img + (size_t)first * is, plane, nb, st);
+   auto ck = [&](cudaError_t e, const char* what) {
+      if (e != cudaSuccess && s == RISA_GB_OK) s = fail(RISA_GB_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+   };
+   if (!lanes2) {
+      for (int first = 0; first < n_frames && s == RISA_GB_OK; first += B) {
+         const int nb = std::min(B, n_frames - first);
+         s = risa_gb_fbp_enqueue(h, raw + (size_t)first * fs, img + (size_t)first * is, plane, nb, st);
+      }
+   } else {
+      // st carries the backprojections, h->s_lane the streaming stages: chunk
+      // c's backprojection waits for its filter; chunk c's filter waits for
+      // the backprojection of chunk c - 2, the last reader of its pair buffer
+      ck(cudaEventRecord(h->ev_fork, st), "fork");
+      ck(cudaStreamWaitEvent(h->s_lane, h->ev_fork, 0), "fork");
+      int c = 0;
+      for (int first = 0; first < n_frames && s == RISA_GB_OK; first += B, ++c) {
+         const int nb = std::min(B, n_frames - first);
+         void* pairs = lane_pairs(h, c & 1);
+         if (c >= 2) ck(cudaStreamWaitEvent(h->s_lane, h->ev_bpl[c & 1], 0), "lane wait");
+         ck(engine_lane_prefix(h, raw + (size_t)first * fs, plane, nb, pairs, h->s_lane), "streaming stages");
+         ck(cudaEventRecord(h->ev_pre, h->s_lane), "lane record");
+         ck(cudaStreamWaitEvent(st, h->ev_pre, 0), "lane wait");
+         ck(engine_lane_bp(h, img + (size_t)first * is, nb, pairs, st), "backprojection");
+         if (s == RISA_GB_OK) {
+            cudaStreamCaptureStatus cs;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd = 0;
+            ck(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd), "capture info");
+            for (size_t i = 0; s == RISA_GB_OK && i < nd; ++i) bp_nodes.push_back(deps[i]);
+         }
+         ck(cudaEventRecord(h->ev_bpl[c & 1], st), "lane record");
+      }
+      // the lane's last work is the event st waited on: it has joined st
    }
    cudaError_t e = cudaStreamEndCapture(st, &graph);
    if (s != RISA_GB_OK) {
@@ -1151,6 +1269,30 @@ static risa_gb_status capture(risa_gb_fbp* h, const uint16_t* raw, float* img, i
       return s;
    }
    if (e != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+   unsigned long long inst_flags = 0;
+   if (lanes2) {
+      // streaming stages at the highest priority, so their blocks are
+      // scheduled as the backprojection's leave the SMs rather than after it
+      int least = 0, greatest = 0;
+      e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+      size_t n = 0;
+      if (e == cudaSuccess) e = cudaGraphGetNodes(graph, nullptr, &n);
+      std::vector<cudaGraphNode_t> nodes(n);
+      if (e == cudaSuccess && n) e = cudaGraphGetNodes(graph, nodes.data(), &n);
+      for (size_t i = 0; e == cudaSuccess && i < n; ++i) {
+         cudaGraphNodeType t;
+         e = cudaGraphNodeGetType(nodes[i], &t);
+         if (e != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+         cudaLaunchAttributeValue v{};
+         v.priority = std::find(bp_nodes.begin(), bp_nodes.end(), nodes[i]) != bp_nodes.end() ? least : greatest;
+         e = cudaGraphKernelNodeSetAttribute(nodes[i], cudaLaunchAttributePriority, &v);
+      }
+      if (e != cudaSuccess) {
+         cudaGraphDestroy(graph);
+         return fail(RISA_GB_ECUDA, std::string("graph priorities: ") + cudaGetErrorString(e));
+      }
+      inst_flags = cudaGraphInstantiateFlagUseNodePriority;
+   }
    if (kernels) {
       size_t n = 0;
       cudaGraphGetNodes(graph, nullptr, &n);
@@ -1164,7 +1306,7 @@ static risa_gb_status capture(risa_gb_fbp* h, const uint16_t* raw, float* img, i
       *kernels = k;
    }
    cudaGraphExec_t exec = nullptr;
-   e = cudaGraphInstantiate(&exec, graph, 0);
+   e = cudaGraphInstantiate(&exec, graph, inst_flags);
    cudaGraphDestroy(graph);
    if (e != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
    *exec_out = exec;
@@ -1198,6 +1340,27 @@ risa_gb_status risa_gb_graph_destroy(risa_gb_graph* g) {
    return RISA_GB_OK;
 }
 
+// Captures one lane's share of a full chunk (B frames) of host slot i on
+// stream st: the streaming stages from raw_slot[i] (bp = false) or the
+// backprojection into img_slot[i] (bp = true), with pair buffer i.
+static risa_gb_status capture_slot_lane(risa_gb_fbp* h, int i, int plane, bool bp, cudaStream_t st,
+                                        cudaGraphExec_t* out) {
+   cudaGraph_t graph = nullptr;
+   RG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+   const cudaError_t e0 = bp ? engine_lane_bp(h, h->img_slot[i].as<float>(), h->max_batch, lane_pairs(h, i), st)
+                             : engine_lane_prefix(h, h->raw_slot[i].as<uint16_t>(), plane, h->max_batch,
+                                                  lane_pairs(h, i), st);
+   const cudaError_t e1 = cudaStreamEndCapture(st, &graph);
+   if (e0 != cudaSuccess || e1 != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return fail(RISA_GB_ECUDA, std::string("slot capture: ") + cudaGetErrorString(e0 != cudaSuccess ? e0 : e1));
+   }
+   const cudaError_t e = cudaGraphInstantiate(out, graph, 0);
+   cudaGraphDestroy(graph);
+   if (e != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("slot instantiate: ") + cudaGetErrorString(e));
+   return RISA_GB_OK;
+}
+
 risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, float* host_img,
                                     int n_frames, int plane) {
    if (!h || !host_raw || !host_img || n_frames < 0) return fail(RISA_GB_EINVAL, "bad arguments");
@@ -1208,25 +1371,21 @@ risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, fl
    if (plane == RISA_GB_PLANES_INTERLEAVED && B % g.L != 0)
       return fail(RISA_GB_EINVAL, "interleaved planes need max_batch to be a multiple of n_planes");
    if (!h->s_comp) {
-      RG_CUDA(cudaStreamCreateWithFlags(&h->s_comp, cudaStreamNonBlocking));
+      // the streaming stages at the highest priority, the backprojection at the lowest
+      int least = 0, greatest = 0;
+      RG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+      RG_CUDA(cudaStreamCreateWithPriority(&h->s_comp, cudaStreamNonBlocking, greatest));
+      RG_CUDA(cudaStreamCreateWithPriority(&h->s_bp, cudaStreamNonBlocking, least));
       RG_CUDA(cudaStreamCreateWithFlags(&h->s_h2d, cudaStreamNonBlocking));
       RG_CUDA(cudaStreamCreateWithFlags(&h->s_d2h, cudaStreamNonBlocking));
       for (int i = 0; i < 2; ++i) {
          RG_CUDA(cudaEventCreateWithFlags(&h->ev_h2d[i], cudaEventDisableTiming));
          RG_CUDA(cudaEventCreateWithFlags(&h->ev_comp[i], cudaEventDisableTiming));
          RG_CUDA(cudaEventCreateWithFlags(&h->ev_d2h[i], cudaEventDisableTiming));
+         RG_CUDA(cudaEventCreateWithFlags(&h->ev_bp_slot[i], cudaEventDisableTiming));
          RG_TRY(h->raw_slot[i].alloc(sizeof(uint16_t) * fs * B));
          RG_TRY(h->img_slot[i].alloc(sizeof(float) * is * B));
       }
-   }
-   if (h->slot_plane != plane) {
-      for (int i = 0; i < 2; ++i) {
-         if (h->slot_exec[i]) cudaGraphExecDestroy(h->slot_exec[i]);
-         h->slot_exec[i] = nullptr;
-         RG_TRY(capture(h, h->raw_slot[i].as<uint16_t>(), h->img_slot[i].as<float>(), plane, B,
-                        h->s_comp, &h->slot_exec[i], nullptr));
-      }
-      h->slot_plane = plane;
    }
    // Chunk sizes: a ramp of B/16 and B/4 frames at both ends, full chunks of
    // B between. Nothing overlaps the first chunk's upload and the last one's
@@ -1254,33 +1413,84 @@ risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, fl
          else sizes.push_back(odd);
       }
    }
+   bool lanes2 = two_lanes(h, B);
+   for (int nb : sizes) lanes2 = lanes2 && two_lanes(h, nb);
+   if (lanes2) RG_TRY(ensure_lanes(h));
+   // (re)capture the slot graphs when the plane mode, the lane mode or a pair
+   // buffer changed since they were captured
+   const void* pk0 = h->bp->pairs.p;
+   const void* pk1 = lanes2 ? h->pairs2.p : nullptr;
+   if (h->slot_plane != plane || h->slot_lanes != (lanes2 ? 2 : 1) || h->slot_pairs[0] != pk0 ||
+       h->slot_pairs[1] != pk1) {
+      for (int i = 0; i < 2; ++i) {
+         if (h->slot_exec[i]) cudaGraphExecDestroy(h->slot_exec[i]);
+         if (h->slot_bp_exec[i]) cudaGraphExecDestroy(h->slot_bp_exec[i]);
+         h->slot_exec[i] = h->slot_bp_exec[i] = nullptr;
+      }
+      h->slot_plane = 0x7fffffff;
+      for (int i = 0; i < 2; ++i) {
+         if (lanes2) {
+            RG_TRY(capture_slot_lane(h, i, plane, false, h->s_comp, &h->slot_exec[i]));
+            RG_TRY(capture_slot_lane(h, i, plane, true, h->s_bp, &h->slot_bp_exec[i]));
+         } else {
+            RG_TRY(capture(h, h->raw_slot[i].as<uint16_t>(), h->img_slot[i].as<float>(), plane, B, h->s_comp,
+                           &h->slot_exec[i], nullptr));
+         }
+      }
+      h->slot_plane = plane;
+      h->slot_lanes = lanes2 ? 2 : 1;
+      h->slot_pairs[0] = pk0;
+      h->slot_pairs[1] = pk1;
+   }
    int first = 0;
    for (size_t c = 0; c < sizes.size(); ++c) {
       const int slot = (int)(c & 1);
       const int nb = sizes[c];
-      // slot buffers are reused every second chunk: wait for their last readers
+      uint16_t* raw_d = h->raw_slot[slot].as<uint16_t>();
+      float* img_d = h->img_slot[slot].as<float>();
+      // the raw slot is reused every second chunk: wait for its last reader
+      // (the streaming stages, or the whole chunk on one lane)
       RG_CUDA(cudaStreamWaitEvent(h->s_h2d, h->ev_comp[slot], 0));
-      RG_CUDA(cudaMemcpyAsync(h->raw_slot[slot].p, host_raw + (size_t)first * fs,
-                              sizeof(uint16_t) * fs * nb, cudaMemcpyHostToDevice, h->s_h2d));
+      RG_CUDA(cudaMemcpyAsync(raw_d, host_raw + (size_t)first * fs, sizeof(uint16_t) * fs * nb,
+                              cudaMemcpyHostToDevice, h->s_h2d));
       RG_CUDA(cudaEventRecord(h->ev_h2d[slot], h->s_h2d));
       RG_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_h2d[slot], 0));
-      RG_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_d2h[slot], 0));
-      // every chunk starts on a plane-0 frame, so a full chunk replays the slot's graph
-      if (nb == B) {
-         RG_CUDA(cudaGraphLaunch(h->slot_exec[slot], h->s_comp));
+      cudaEvent_t done;  // the image slot is complete after this event
+      if (lanes2) {
+         // pair buffer `slot`: its last reader is the backprojection of chunk c - 2
+         RG_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_bp_slot[slot], 0));
+         if (nb == B) RG_CUDA(cudaGraphLaunch(h->slot_exec[slot], h->s_comp));
+         else RG_CUDA(engine_lane_prefix(h, raw_d, plane, nb, lane_pairs(h, slot), h->s_comp));
+         RG_CUDA(cudaEventRecord(h->ev_comp[slot], h->s_comp));
+         RG_CUDA(cudaStreamWaitEvent(h->s_bp, h->ev_comp[slot], 0));
+         RG_CUDA(cudaStreamWaitEvent(h->s_bp, h->ev_d2h[slot], 0));  // the image slot's last reader
+         if (nb == B) RG_CUDA(cudaGraphLaunch(h->slot_bp_exec[slot], h->s_bp));
+         else RG_CUDA(engine_lane_bp(h, img_d, nb, lane_pairs(h, slot), h->s_bp));
+         RG_CUDA(cudaEventRecord(h->ev_bp_slot[slot], h->s_bp));
+         done = h->ev_bp_slot[slot];
       } else {
-         RG_TRY(risa_gb_fbp_enqueue(h, h->raw_slot[slot].as<uint16_t>(), h->img_slot[slot].as<float>(),
-                                    plane, nb, h->s_comp));
+         RG_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_d2h[slot], 0));
+         // every chunk starts on a plane-0 frame, so a full chunk replays the slot's graph
+         if (nb == B) RG_CUDA(cudaGraphLaunch(h->slot_exec[slot], h->s_comp));
+         else RG_TRY(risa_gb_fbp_enqueue(h, raw_d, img_d, plane, nb, h->s_comp));
+         RG_CUDA(cudaEventRecord(h->ev_comp[slot], h->s_comp));
+         done = h->ev_comp[slot];
       }
-      RG_CUDA(cudaEventRecord(h->ev_comp[slot], h->s_comp));
-      RG_CUDA(cudaStreamWaitEvent(h->s_d2h, h->ev_comp[slot], 0));
-      RG_CUDA(cudaMemcpyAsync(host_img + (size_t)first * is, h->img_slot[slot].p, sizeof(float) * is * nb,
+      RG_CUDA(cudaStreamWaitEvent(h->s_d2h, done, 0));
+      RG_CUDA(cudaMemcpyAsync(host_img + (size_t)first * is, img_d, sizeof(float) * is * nb,
                               cudaMemcpyDeviceToHost, h->s_d2h));
       RG_CUDA(cudaEventRecord(h->ev_d2h[slot], h->s_d2h));
       first += nb;
    }
    RG_CUDA(cudaStreamSynchronize(h->s_d2h));
+   RG_CUDA(cudaStreamSynchronize(h->s_bp));
    RG_CUDA(cudaStreamSynchronize(h->s_comp));
+   return RISA_GB_OK;
+}
+
+risa_gb_status risa_gb_fbp_set_lanes(risa_gb_fbp* h, int lanes) {
+   if (!h || (lanes != 1 && lanes != 2)) return fail(RISA_GB_EINVAL, "lanes must be 1 or 2");
+   h->lanes = lanes;
    return RISA_GB_OK;
 }
 

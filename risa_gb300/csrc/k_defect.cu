@@ -3,9 +3,12 @@
 // The reference runs this on the host with a device->host->device round trip
 // per frame (DetectorInterpolation.cu:113-139) using findDefectDetectors and
 // interpolateDefectDetectors (interpolationFunctions.h:28-97). Here:
-//   1. defect_stats: per-column total variation (exact integer sum, so the
-//      result does not depend on the reduction order) and max/min, reduced
-//      over row chunks with integer atomics;
+//   1. defect_stats_cluster (detector-major frames): per-column total
+//      variation (exact integer sum, so the result does not depend on the
+//      reduction order) and max/min; a cluster of 8 CTAs covers one frame,
+//      one row chunk each, and the chunks are combined through distributed
+//      shared memory (no atomics, no zeroing pass); defect_stats (module-major
+//      frames) reduces its row chunks with integer atomics instead;
 //   2. defect_flags: one CTA per frame forms var = TV * range^2 in FP64,
 //      applies the 17-tap threshold with the reference's exact operation
 //      order (no FMA contraction) and compiles the ordered list of defect
@@ -13,6 +16,8 @@
 //   3. defect_repair (or the attenuation kernel, fused): each row applies the
 //      runs in list order, so in-place dependencies between runs resolve as
 //      in the reference's sequential loop.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 
 #include "kernels.h"
@@ -63,56 +68,92 @@ __global__ void __launch_bounds__(kStatThreads) defect_stats(const uint16_t* __r
    atomicMin(&s->mn, mn);
 }
 
-// Detector-major frames with D % 8 == 0 and 16-byte aligned rows: each thread
-// takes 8 adjacent columns (one 16-byte load per row), keeps their max/min as
+// Detector-major frames with D % 8 == 0 and 16-byte aligned rows. A cluster
+// of kStatCluster CTAs owns one frame and one block of column octets; CTA r
+// of the cluster takes row chunk r. Each thread takes 8 adjacent columns (one
+// 16-byte load per row, kStatBatch rows in flight), keeps their max/min as
 // packed 16-bit pairs and their total variation in 32 bits (at most
-// `rows` * 65535 per chunk, rows <= 32768), and adds the chunk's results
-// atomically. Rows are loaded kStatBatch at a time so that many loads are in
-// flight. Each chunk ends in 6 atomics per column, so large batches take
-// longer chunks (fewer atomics) while the grid stays large (the launcher).
-constexpr int kStatRowsVec = 64;  // shortest chunk
+// `rows` * 65535 per chunk, rows <= 32768), and leaves them in shared memory;
+// after a cluster barrier CTA 0 sums the chunks in 64 bits, reading the other
+// CTAs' shared memory, and writes the column statistics. Every CTA reaches
+// both cluster barriers (no early return), and a cluster's CTAs are
+// co-scheduled, so the barriers always complete.
+constexpr int kStatCluster = 8;
+constexpr int kStatMaxThreads = 256;
 constexpr int kStatBatch = 8;
-__global__ void __launch_bounds__(256) defect_stats_vec8(const uint16_t* __restrict__ frames,
-                                                         ColStats* __restrict__ st, int P, int D, int rows) {
-   const int o = blockIdx.x * blockDim.x + threadIdx.x;  // column octet
-   if (8 * o >= D) return;
-   const int r0 = blockIdx.y * rows;
+__global__ void __cluster_dims__(kStatCluster, 1, 1) __launch_bounds__(kStatMaxThreads)
+    defect_stats_cluster(const uint16_t* __restrict__ frames, ColStats* __restrict__ st, int P, int D, int rows) {
+   __shared__ uint32_t part[16][kStatMaxThreads];  // tv[8], mx[4], mn[4] of every thread
+   namespace cg = cooperative_groups;
+   cg::cluster_group cl = cg::this_cluster();
+   const unsigned rank = cl.block_rank();
+   const int t = threadIdx.x;
+   const int o = (blockIdx.x / kStatCluster) * blockDim.x + t;  // column octet
+   const bool act = 8 * o < D;
+   const int r0 = (int)rank * rows;
    const int r1 = min(r0 + rows, P - 1);  // pairs (p, p+1) with p < r1
-   if (r0 >= r1) return;
-   const uint4* f = reinterpret_cast<const uint4*>(frames + (size_t)blockIdx.z * P * D) + o;
-   const size_t rs = (size_t)D / 8;
-   uint4 prev = __ldg(f + (size_t)r0 * rs);
-   uint32_t mx[4] = {prev.x, prev.y, prev.z, prev.w}, mn[4] = {prev.x, prev.y, prev.z, prev.w};
+   uint32_t mx[4] = {0u, 0u, 0u, 0u}, mn[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
    uint32_t tv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-   for (int p = r0; p < r1; p += kStatBatch) {
-      uint4 nx[kStatBatch];
+   if (act && r0 < r1) {
+      const uint4* f = reinterpret_cast<const uint4*>(frames + (size_t)blockIdx.z * P * D) + o;
+      const size_t rs = (size_t)D / 8;
+      uint4 prev = __ldg(f + (size_t)r0 * rs);
+      for (int p = r0; p < r1; p += kStatBatch) {
+         uint4 nx[kStatBatch];
 #pragma unroll
-      for (int i = 0; i < kStatBatch; ++i)
-         nx[i] = (p + i < r1) ? __ldg(f + (size_t)(p + 1 + i) * rs) : prev;
+         for (int i = 0; i < kStatBatch; ++i)
+            nx[i] = (p + i < r1) ? __ldg(f + (size_t)(p + 1 + i) * rs) : prev;
 #pragma unroll
-      for (int i = 0; i < kStatBatch; ++i) {
-         if (p + i >= r1) break;
-         const uint32_t a[4] = {prev.x, prev.y, prev.z, prev.w}, b[4] = {nx[i].x, nx[i].y, nx[i].z, nx[i].w};
+         for (int i = 0; i < kStatBatch; ++i) {
+            if (p + i >= r1) break;
+            const uint32_t a[4] = {prev.x, prev.y, prev.z, prev.w}, b[4] = {nx[i].x, nx[i].y, nx[i].z, nx[i].w};
 #pragma unroll
-         for (int j = 0; j < 4; ++j) {
-            tv[2 * j] = __sad(a[j] & 0xFFFFu, b[j] & 0xFFFFu, tv[2 * j]);
-            tv[2 * j + 1] = __sad(a[j] >> 16, b[j] >> 16, tv[2 * j + 1]);
-            mx[j] = __vmaxu2(mx[j], a[j]);
-            mn[j] = __vminu2(mn[j], a[j]);
+            for (int j = 0; j < 4; ++j) {
+               tv[2 * j] = __sad(a[j] & 0xFFFFu, b[j] & 0xFFFFu, tv[2 * j]);
+               tv[2 * j + 1] = __sad(a[j] >> 16, b[j] >> 16, tv[2 * j + 1]);
+               mx[j] = __vmaxu2(mx[j], a[j]);
+               mn[j] = __vminu2(mn[j], a[j]);
+            }
+            prev = nx[i];
          }
-         prev = nx[i];
       }
    }
-   ColStats* s = st + (size_t)blockIdx.z * D + 8 * o;
+#pragma unroll
+   for (int k = 0; k < 8; ++k) part[k][t] = tv[k];
 #pragma unroll
    for (int j = 0; j < 4; ++j) {
-      atomicAdd(&s[2 * j].tv, (unsigned long long)tv[2 * j]);
-      atomicAdd(&s[2 * j + 1].tv, (unsigned long long)tv[2 * j + 1]);
-      atomicMax(&s[2 * j].mx, mx[j] & 0xFFFFu);
-      atomicMax(&s[2 * j + 1].mx, mx[j] >> 16);
-      atomicMin(&s[2 * j].mn, mn[j] & 0xFFFFu);
-      atomicMin(&s[2 * j + 1].mn, mn[j] >> 16);
+      part[8 + j][t] = mx[j];
+      part[12 + j][t] = mn[j];
    }
+   cl.sync();
+   if (rank == 0 && act) {
+      unsigned long long s64[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      uint32_t MX[4] = {0u, 0u, 0u, 0u}, MN[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+      for (int q = 0; q < kStatCluster; ++q) {
+         const uint32_t* rp = cl.map_shared_rank(&part[0][0], q);
+#pragma unroll
+         for (int k = 0; k < 8; ++k) s64[k] += rp[k * kStatMaxThreads + t];
+#pragma unroll
+         for (int j = 0; j < 4; ++j) {
+            MX[j] = __vmaxu2(MX[j], rp[(8 + j) * kStatMaxThreads + t]);
+            MN[j] = __vminu2(MN[j], rp[(12 + j) * kStatMaxThreads + t]);
+         }
+      }
+      ColStats* s = st + (size_t)blockIdx.z * D + 8 * o;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+         ColStats lo, hi;
+         lo.tv = s64[2 * j];
+         lo.mx = MX[j] & 0xFFFFu;
+         lo.mn = MN[j] & 0xFFFFu;
+         hi.tv = s64[2 * j + 1];
+         hi.mx = MX[j] >> 16;
+         hi.mn = MN[j] >> 16;
+         s[2 * j] = lo;
+         s[2 * j + 1] = hi;
+      }
+   }
+   cl.sync();  // the other CTAs' shared memory stays alive until CTA 0 has read it
 }
 
 // One CTA per frame. Dynamic shared memory: var[D] (double) then flags[D+1].
@@ -312,18 +353,16 @@ cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const Defect
                                  DefectWorkspace ws, int32_t* flags_out, cudaStream_t st) {
    if (batch <= 0) return cudaSuccess;
    const int n = cfg.D * batch;
-   defect_stats_init<<<(n + 255) / 256, 256, 0, st>>>(ws.stats, n);
-   if (cfg.modules <= 0 && cfg.D % 8 == 0 && ((uintptr_t)frames & 15u) == 0) {
-      // one block spans a frame's column octets where it can (D <= 2048)
+   if (cfg.modules <= 0 && cfg.D % 8 == 0 && ((uintptr_t)frames & 15u) == 0 && cfg.P - 1 <= 8 * 32768) {
+      // one block spans a frame's column octets where it can (D <= 2048);
+      // the cluster's CTAs split the rows
       const int octets = cfg.D / 8;
-      const int threads = std::min(256, (octets + 31) / 32 * 32);
-      // double the chunk while the grid keeps at least 1024 CTAs
-      int rows = kStatRowsVec;
-      auto ctas = [&](int r) { return (long long)batch * ((cfg.P - 1 + r - 1) / r) * ((octets + threads - 1) / threads); };
-      while (rows < cfg.P - 1 && rows < 32768 && ctas(2 * rows) >= 1024) rows *= 2;
-      dim3 grid((octets + threads - 1) / threads, (cfg.P - 1 + rows - 1) / rows, batch);
-      defect_stats_vec8<<<grid, threads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D, rows);
+      const int threads = std::min(kStatMaxThreads, (octets + 31) / 32 * 32);
+      const int rows = std::max(1, (cfg.P - 1 + kStatCluster - 1) / kStatCluster);
+      dim3 grid(kStatCluster * ((octets + threads - 1) / threads), 1, batch);
+      defect_stats_cluster<<<grid, threads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D, rows);
    } else {
+      defect_stats_init<<<(n + 255) / 256, 256, 0, st>>>(ws.stats, n);
       dim3 grid((cfg.D + kStatThreads - 1) / kStatThreads, (cfg.P - 1 + kStatRows - 1) / kStatRows,
                 batch);
       defect_stats<<<grid, kStatThreads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D, cfg.modules);

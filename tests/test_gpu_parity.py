@@ -405,6 +405,51 @@ def test_graph_replay_and_host_path_match_enqueue():
     assert rel_err(got3[n - 2], expect[n - 2])[0] < MAX_REL
 
 
+@pytest.mark.parametrize("variant", ["staged_cp_s4_a8_p4", "staged_s2_a16_p4", "pairs_s2_a32"])
+def test_two_lanes_match_one_lane(variant):
+    """Graphs and the host path with one chunk's backprojection beside the next
+    chunk's streaming stages (two lanes, two pair buffers) give the same bits
+    as every stage in sequence; variants whose backprojection reads the
+    rebinned sinogram itself run on one lane either way."""
+    L = 2
+    d = dict(SMALL, n_planes=L, source_diameter=[430.0] * L, delta_x=[0.0] * L, delta_z=[1417.0, 1430.0],
+             source_angle=[360.0] * L, n_par_proj=128, n_par_det=256, n_pixels=128)
+    sc = phantom.make_scan(8, L, 500, 432, 215.0, 240.0, seed=31, defect_fraction=0.01, distinct=8)
+    n, N, B = sc.raw.shape[0], d["n_pixels"], 4  # 4 graph chunks; host chunks 2, 2, 4, 4, 2, 2
+    g = geom(d)
+    p = rg.make_params(filter_type="sheppLogan", defects=True, masking=True)
+    v = [rg.Backprojection.variant_name(i) for i in range(rg.Backprojection.variant_count())].index(variant)
+    raw = dev(sc.raw.view(np.int16))
+    hraw = torch.from_numpy(sc.raw.view(np.int16)).pin_memory()
+    out = {}
+    for lanes in (1, 2):
+        fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=B)
+        fbp.backprojection().set_variant(v)
+        fbp.set_lanes(lanes)
+        direct = torch.empty((n, N, N), dtype=torch.float32, device="cuda")
+        for c in range(0, n, B):
+            fbp.enqueue(raw[c:c + B], direct[c:c + B], rg.PLANES_INTERLEAVED, B)
+        s = torch.cuda.Stream()
+        img = torch.full((n, N, N), float("nan"), dtype=torch.float32, device="cuda")
+        graph = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, s)
+        for _ in range(2):
+            graph.replay(s)
+        s.synchronize()
+        himg = torch.full((n, N, N), float("nan"), dtype=torch.float32).pin_memory()
+        fbp.run_host(hraw, himg, n, rg.PLANES_INTERLEAVED)
+        fbp.backprojection().check()
+        out[lanes] = (host(direct), img.cpu().numpy(), himg.numpy())
+    ref = out[1][0]
+    for lanes in (1, 2):
+        for what, got in zip(("enqueue", "graph", "host path"), out[lanes]):
+            np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32), err_msg=f"{lanes} lanes, {what}")
+    ref_o, dark_o = oracle.attenuation_init(sc.ref, sc.dark, L, 0.67, 1.5, True, oracle.QUIRK_NONE)
+    op = oracle.make_params(quirk=oracle.QUIRK_NONE, filter_type="sheppLogan", defects=True, masking=True)
+    exp = oracle.fbp(ns(d), op, oracle.f2p_records(ns(d), oracle.QUIRK_NONE), ref_o, dark_o, sc.raw[:4], sc.planes[:4])
+    for i in range(4):
+        assert rel_err(ref[i], exp[i])[0] < MAX_REL, i
+
+
 def test_errors_are_reported():
     g = rg.make_geometry(n_par_proj=16, n_par_det=16, n_pixels=16)
     bp = rg.Backprojection(g, rg.make_params())
