@@ -304,8 +304,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         "config": {"workload": WORKLOAD_NAME, "frames_per_plane": args.frames, "slices_per_step": job_frames,
                    "slices_per_rank": n,
                    "batch": B, "bp_variant": variant,
-                   "graph": "one CUDA graph per step, two lanes (a chunk's backprojection beside the next "
-                            "chunk's streaming stages)",
+                   "graph": "one CUDA graph per step, the stages of each chunk in sequence (one lane)",
                    "l2": "inputs larger than L2 (%.1f GB raw per step)" % (sc.raw.nbytes / 1e9),
                    "parallelism": f"replicas x{world}"},
         "gpu_launches": launches_per_step * args.steps,
@@ -434,16 +433,22 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
         "hbm_peak_gbs": hbm, "batch": B,
     }
 
-    # ---- the same job as one lane: every stage of a chunk in sequence, no
-    # backprojection beside the next chunk's streaming stages
-    fbp.set_lanes(1)
-    g1 = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, stream)
-    ms1 = timed(torch, stream, lambda: g1.replay(stream), 2)
+    # ---- the same job as two lanes: each chunk's backprojection beside the
+    # next chunk's streaming stages (the headline runs them in sequence)
     fbp.set_lanes(2)
-    out["one_lane"] = {"value": n / (ms1 / 1e3), "unit": "slices/s", "ms_per_step": ms1,
-                       "graph_kernels": g1.kernel_count,
-                       "how": "the headline's graph captured with risa_gb_fbp_set_lanes(1), CUDA events"}
-    del g1
+    g2 = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, stream)
+    ms2 = timed(torch, stream, lambda: g2.replay(stream), 2)
+    fbp.set_lanes(1)
+    out["two_lanes"] = {"value": n / (ms2 / 1e3), "unit": "slices/s", "ms_per_step": ms2,
+                        "graph_kernels": g2.kernel_count,
+                        "how": "the headline's job captured with risa_gb_fbp_set_lanes(2), CUDA events"}
+    del g2
+    # the sum of the stages' isolated times over the job's chunks, against the
+    # graph's step time: what a single persistent launch could save at most
+    # without running stages concurrently
+    chunks = n / B
+    out["graph_overhead"] = {"sum_of_stage_ms_per_step": sum(es.values()) * chunks,
+                             "chunks_per_step": chunks}
 
     # ---- plain per-stage path: one frame per launch, sync after every stage
     dfx = rg.Defects(g, p, max_batch=1)
@@ -727,6 +732,9 @@ def measure_sweep(torch, rg, dev):
     img = torch.empty(it, dtype=torch.float32, device=dev)
     ms = cuda_ms(torch, lambda: sw.enqueue(raw, img))
     sw.check()
+    graph = sw.graph_capture(raw, img, torch.cuda.Stream(device=dev))
+    ms_graph = cuda_ms(torch, lambda: graph.replay(None))
+    sw.check()
     first, done, launch = sw.times()
     span = (done - first) / 1e6
     comp = (done - launch) / 1e6
@@ -749,7 +757,7 @@ def measure_sweep(torch, rg, dev):
     return {"workload": "256 instances: side log-uniform 128..1024, angles 180..1440, rays 1.25 x side "
                         "(multiple of 32), 0..2% defective columns, Ram-Lak or Hann, circular mask",
             "ms_per_launch": ms, "instances_per_s": 256 / (ms / 1e3), "gupdates_per_s": upd / (ms / 1e3) / 1e9,
-            "grid": sw.grid(), "launches": 1,
+            "ms_per_graph_replay": ms_graph, "grid": sw.grid(), "launches": 1,
             "instance_span_ms": {"p50": float(np.percentile(span, 50)), "p99": float(np.percentile(span, 99))},
             "completion_ms": {"p50": float(np.percentile(comp, 50)), "p99": float(np.percentile(comp, 99))},
             "max_rel_vs_fp64_4_smallest": worst}

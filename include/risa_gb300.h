@@ -372,7 +372,7 @@ risa_gb_status risa_gb_fbp_enqueue(risa_gb_fbp* h, const uint16_t* raw, float* i
  * in chunks of max_batch through the handle's buffers) as one CUDA graph with
  * fixed device pointers. Replaying it reruns the whole job with a single
  * launch. With interleaved planes, max_batch must be a multiple of n_planes.
- * With two lanes (risa_gb_fbp_set_lanes; the default) and more than one
+ * With two lanes (risa_gb_fbp_set_lanes) and more than one
  * chunk, chunk c's backprojection runs beside chunk c+1's defect detection,
  * attenuation, rebinning and filter, which run at the highest stream priority;
  * the two lanes alternate between two pair-record buffers. The graph uses the
@@ -394,11 +394,12 @@ risa_gb_status risa_gb_graph_destroy(risa_gb_graph* g);
  * copies the images back. Pinned host memory is fastest. Blocks until done. */
 risa_gb_status risa_gb_fbp_run_host(risa_gb_fbp* h, const uint16_t* host_raw, float* host_img,
                                     int n_frames, int plane);
-/* 2 (the default): chunks run as two lanes where the filter writes the
- * backprojection's pair records (staged variants; otherwise one lane); 1:
- * every stage of a chunk in sequence on one stream. Applies to later graph
- * captures and host-path calls; results are identical either way. No
- * reference counterpart (the reference runs one frame per stage call). */
+/* 1 (the default): every stage of a chunk in sequence on one stream; 2:
+ * chunks run as two lanes where the filter writes the backprojection's pair
+ * records (staged variants; otherwise one lane), chunk c's backprojection
+ * beside chunk c+1's streaming stages. Applies to later graph captures and
+ * host-path calls; results are identical either way. No reference
+ * counterpart (the reference runs one frame per stage call). */
 risa_gb_status risa_gb_fbp_set_lanes(risa_gb_fbp* h, int lanes);
 /* Per-stage access for inspection (intermediate device buffers). The engine
  * keeps attenuated fan frames as frame quads -- 4 frames of one plane side by
@@ -452,6 +453,12 @@ risa_gb_status risa_gb_sweep_layout(const risa_gb_sweep* h, size_t* raw_offsets,
                                     size_t* raw_total, size_t* img_total);
 /* One persistent launch over every instance (device buffers, packed as above). */
 risa_gb_status risa_gb_sweep_enqueue(risa_gb_sweep* h, const uint16_t* raw, float* img, void* stream);
+/* The enqueue above (its counter resets and the persistent launch) captured as
+ * a CUDA graph on `stream` (non-default), replayed with risa_gb_graph_replay
+ * and freed with risa_gb_graph_destroy. The graph uses the handle's work
+ * counters: do not replay it concurrently with other work on the handle. */
+risa_gb_status risa_gb_sweep_graph_capture(risa_gb_sweep* h, const uint16_t* raw, float* img, void* stream,
+                                          risa_gb_graph** out);
 /* Synchronises; per instance the %globaltimer time (ns) its first row group
  * started and its last tile finished in the last enqueue, and the launch's
  * earliest CTA start. Any pointer may be NULL. */

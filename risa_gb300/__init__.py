@@ -151,6 +151,7 @@ SIGNATURES = {
     "risa_gb_sweep_grid": (_i, [_vp]),
     "risa_gb_measure_peak": (_i, [_i, _i, _vp, ctypes.POINTER(ctypes.c_double)]),
     "risa_gb_fbp_set_lanes": (_i, [_vp, _i]),
+    "risa_gb_sweep_graph_capture": (_i, [_vp, _vp, _vp, _vp, _pp]),
     "risa_gb_assembler_create": (_i, [_vp, _vp, _i, _i, _pp]),
     "risa_gb_assembler_ingest": (_i, [_vp, _i, ctypes.c_char_p, _sz]),
     "risa_gb_assembler_next": (_i, [_vp, _d, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int)]),
@@ -611,8 +612,9 @@ class FBP(_Handle):
                "fbp_run_host")
 
     def set_lanes(self, lanes: int):
-        """2 (default): one chunk's backprojection beside the next chunk's
-        streaming stages in graphs and the host path; 1: stages in sequence."""
+        """1 (default): every stage of a chunk in sequence; 2: one chunk's
+        backprojection beside the next chunk's streaming stages, in graphs and
+        the host path (same results)."""
         _check(lib().risa_gb_fbp_set_lanes(self._h, lanes), "fbp_set_lanes")
 
     def intermediates(self):
@@ -758,6 +760,14 @@ class Sweep(_Handle):
 
     def enqueue(self, raw, img, stream=None):
         _check(lib().risa_gb_sweep_enqueue(self._h, ptr(raw), ptr(img), stream_ptr(stream)), "sweep_enqueue")
+
+    def graph_capture(self, raw, img, stream) -> "Graph":
+        """The enqueue (counter resets + the persistent launch) as one CUDA graph."""
+        gr = Graph()
+        _check(lib().risa_gb_sweep_graph_capture(self._h, ptr(raw), ptr(img), stream_ptr(stream),
+                                                 ctypes.byref(gr._h)), "sweep_graph_capture")
+        gr.owner = self
+        return gr
 
     def times(self):
         """(first_ns[n], done_ns[n], launch_ns) of the last enqueue (%globaltimer)."""

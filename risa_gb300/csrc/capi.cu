@@ -231,7 +231,7 @@ struct risa_gb_backprojection {
    DevBuf pairs, err;
    DevBuf rowbase, colbase;  // adjoint: (hi, lo) line starts [Pp][N]
    DevBuf adj;               // adjoint: slice-interleaved image copies (reserve_adjoint)
-   DevBuf tile_win;          // staged variants: window start + origin per tile and angle
+   DevBuf tile_win, tile_win64;  // staged variants: window start + origin per 32 / 64 tile and angle
    std::vector<float> a_host, b_host;  // the staged variants' kernel-parameter copies of a and b
    BPCfg cfg(bool fused_mask) const {
       BPCfg c;
@@ -255,6 +255,7 @@ struct risa_gb_backprojection {
       c.rowbase = rowbase.as<float2>();
       c.colbase = colbase.as<float2>();
       c.tile_win = tile_win.as<int2>();
+      c.tile_win64 = tile_win64.as<int2>();
       c.adj_scratch = adj.p;
       c.adj_scratch_bytes = adj.bytes;
       return c;
@@ -280,14 +281,6 @@ struct risa_gb_masking {
    Params p;
 };
 
-struct risa_gb_graph {
-   cudaGraphExec_t exec = nullptr;
-   int kernels = 0;
-   ~risa_gb_graph() {
-      if (exec) cudaGraphExecDestroy(exec);
-   }
-};
-
 struct risa_gb_fbp {
    Geometry g;
    Params p;
@@ -303,8 +296,11 @@ struct risa_gb_fbp {
    // records): chunk c's backprojection runs beside chunk c+1's streaming
    // stages (defects, attenuation, rebinning, filter), which run at a higher
    // stream priority; consecutive chunks alternate between two pair buffers.
-   // lanes = 1 runs every stage of a chunk in sequence.
-   int lanes = 2;
+   // lanes = 1 (the default) runs every stage of a chunk in sequence: on the
+   // full-rate workload it measured 0.6% faster (the stages compete for the
+   // same SM resources; the one-lane graph already runs at the sum of its
+   // kernels' times).
+   int lanes = 1;
    DevBuf pairs2;                  // the second pair buffer (the first is the backprojection's own)
    cudaStream_t s_lane = nullptr;  // graph capture: the streaming-stage lane
    cudaEvent_t ev_fork = nullptr, ev_pre = nullptr, ev_bpl[2] = {nullptr, nullptr};
@@ -809,9 +805,12 @@ risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* gi, const r
       // 8 B per tile and angle (2 MB for 512^2 x 1024 angles); very large
       // geometries keep computing the window starts on the device instead
       const size_t tiles = (size_t)((h->g.N + 31) / 32) * ((h->g.N + 31) / 32);
-      if (tiles * (size_t)h->g.Pp * sizeof(int2) <= ((size_t)256 << 20))
+      if (tiles * (size_t)h->g.Pp * sizeof(int2) <= ((size_t)256 << 20)) {
          RG_TRY(h->tile_win.upload(bp_tile_windows(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(), t.t0.data(),
-                                                   h->g.Pp, h->g.N)));
+                                                   h->g.Pp, h->g.N, 32)));
+         RG_TRY(h->tile_win64.upload(bp_tile_windows(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(),
+                                                     t.t0.data(), h->g.Pp, h->g.N, 64)));
+      }
       RG_TRY(h->rowbase.upload(bp_line_starts(t.t0.data(), t.bd.data(), h->g.Pp, h->g.N)));
       RG_TRY(h->colbase.upload(bp_line_starts(t.t0.data(), t.ad.data(), h->g.Pp, h->g.N)));
    }

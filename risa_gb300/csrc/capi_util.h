@@ -61,3 +61,12 @@ struct DevBuf {
 inline cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
 
 }  // namespace risa_gb
+
+// An instantiated CUDA graph of the engine or of the sweep (risa_gb_graph_*).
+struct risa_gb_graph {
+   cudaGraphExec_t exec = nullptr;
+   int kernels = 0;
+   ~risa_gb_graph() {
+      if (exec) cudaGraphExecDestroy(exec);
+   }
+};

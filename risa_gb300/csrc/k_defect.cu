@@ -29,6 +29,7 @@ namespace {
 constexpr int kStatThreads = 128;
 constexpr int kStatRows = 128;
 __constant__ double c_defect_filter[9];
+__constant__ float c_defect_filter32[9];  // the same weights rounded to float (the FP32 screen)
 
 __global__ void defect_stats_init(ColStats* st, int n) {
    const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -156,7 +157,20 @@ __global__ void __cluster_dims__(kStatCluster, 1, 1) __launch_bounds__(kStatMaxT
    cl.sync();  // the other CTAs' shared memory stays alive until CTA 0 has read it
 }
 
-// One CTA per frame. Dynamic shared memory: var[D] (double) then flags[D+1].
+// One CTA per frame. Dynamic shared memory: var[D] (double), var32[D] (the
+// same rounded to float), flags[D+1].
+//
+// The flags depend only on the comparisons var < thresh_min * th and
+// var > thresh_max * th, where th is the 17-tap threshold the reference forms
+// in FP64 with its own operation order. GB300's FP64 rate is low (~2 FMA per
+// clock and SM), so the threshold is first formed in FP32 (th32: 18 non-negative
+// products, relative error below 22 float roundings, 1.4e-6) and a comparison is
+// settled by it when var lies more than kScreenMargin (1e-5, relative) away from
+// the FP32 bound; only columns inside that band, which the FP32 value cannot
+// decide, take the FP64 sequence. With positive thresholds the settled
+// outcomes equal the FP64 ones: a bound within 1.4e-6 of the FP64 product and
+// a var rounded to float (6e-8) cannot move across a 1e-5 margin.
+constexpr float kScreenMargin = 1e-5f;
 __global__ void defect_flags(const ColStats* __restrict__ st, DefectCfg cfg,
                              int32_t* __restrict__ flags_out, int* __restrict__ counts,
                              DefectRun* __restrict__ runs, int* __restrict__ fix_counts,
@@ -164,37 +178,66 @@ __global__ void defect_flags(const ColStats* __restrict__ st, DefectCfg cfg,
    extern __shared__ double smem_d[];
    const int D = cfg.D;
    double* var = smem_d;
-   int* flags = reinterpret_cast<int*>(var + D);
+   float* var32 = reinterpret_cast<float*>(var + D);
+   int* flags = reinterpret_cast<int*>(var32 + D);
    const int f = blockIdx.x;
    const ColStats* s = st + (size_t)f * D;
    for (int d = threadIdx.x; d < D; d += blockDim.x) {
       const unsigned long long range = (unsigned long long)(s[d].mx - s[d].mn);
-      var[d] = __dmul_rn((double)s[d].tv, (double)(range * range));
+      const double v = __dmul_rn((double)s[d].tv, (double)(range * range));
+      var[d] = v;
+      var32[d] = __double2float_rn(v);
       flags[d] = 0;
    }
    if (threadIdx.x == 0) flags[D] = 0;
    __syncthreads();
    const unsigned H = (unsigned)D / 2u;
+   const bool risa = cfg.quirk == RISA_GB_QUIRKS_RISA;
+   const bool screen = cfg.thresh_min > 0.0 && cfg.thresh_max > 0.0;
+   const float tmin32 = (float)cfg.thresh_min, tmax32 = (float)cfg.thresh_max;
    for (unsigned t = threadIdx.x; t < 2u * H; t += blockDim.x) {
-      const unsigned seg = t / H, i = t % H;
-      double th = 0.0;
+      const unsigned seg = t / H, i = t - seg * H, base = seg * H;
+      // the taps' columns within the half ring: i - j and i + j modulo H
+      unsigned i1[9], i2[9];
 #pragma unroll
       for (unsigned j = 0; j < 9u; ++j) {
-         unsigned i1;
-         if (cfg.quirk == RISA_GB_QUIRKS_RISA)
-            i1 = (i - j) % H;  // unsigned wrap, interpolationFunctions.h:53
+         if (risa)
+            i1[j] = (i - j) % H;  // unsigned wrap, interpolationFunctions.h:53
          else
-            i1 = (i + H * 9u - j) % H;
-         const unsigned i2 = (i + j) % H;
-         th = __dadd_rn(th, __dmul_rn(c_defect_filter[j], var[i1 + seg * H]));
-         th = __dadd_rn(th, __dmul_rn(c_defect_filter[j], var[i2 + seg * H]));
+            i1[j] = H > 8u ? (i >= j ? i - j : i + H - j) : (i + H * 9u - j) % H;
+         i2[j] = H > 8u ? (i + j < H ? i + j : i + j - H) : (i + j) % H;
       }
-      const unsigned det = seg * H + i;
-      if (var[det] < __dmul_rn(cfg.thresh_min, th)) flags[det] = 1;
-      if (var[det] > __dmul_rn(cfg.thresh_max, th)) {
+      const unsigned det = base + i;
+      const double v = var[det];
+      int low = -1, high = -1;  // -1: not settled by the FP32 screen
+      if (screen) {
+         float th32 = 0.f;
+#pragma unroll
+         for (unsigned j = 0; j < 9u; ++j) {
+            th32 = fmaf(c_defect_filter32[j], var32[i1[j] + base], th32);
+            th32 = fmaf(c_defect_filter32[j], var32[i2[j] + base], th32);
+         }
+         const float v32 = var32[det], lo = tmin32 * th32, hi = tmax32 * th32;
+         if (v32 < lo * (1.f - kScreenMargin)) low = 1;
+         else if (v32 > lo * (1.f + kScreenMargin)) low = 0;
+         if (v32 > hi * (1.f + kScreenMargin)) high = 1;
+         else if (v32 < hi * (1.f - kScreenMargin)) high = 0;
+      }
+      if (low < 0 || high < 0) {
+         double th = 0.0;
+#pragma unroll
+         for (unsigned j = 0; j < 9u; ++j) {
+            th = __dadd_rn(th, __dmul_rn(c_defect_filter[j], var[i1[j] + base]));
+            th = __dadd_rn(th, __dmul_rn(c_defect_filter[j], var[i2[j] + base]));
+         }
+         low = v < __dmul_rn(cfg.thresh_min, th);
+         high = v > __dmul_rn(cfg.thresh_max, th);
+      }
+      if (low) flags[det] = 1;
+      if (high) {
          for (int off = -2; off <= 2; ++off) {
             unsigned k;
-            if (cfg.quirk == RISA_GB_QUIRKS_RISA)
+            if (risa)
                k = (det + (unsigned)off) % (unsigned)D;
             else
                k = (det + (unsigned)D + (unsigned)off) % (unsigned)D;
@@ -341,12 +384,18 @@ cudaError_t upload_defect_filter(cudaStream_t st) {
    for (double v : raw) sum += v;
    const double inv = 1.0 / sum;
    double f[9];
-   for (int i = 0; i < 9; ++i) f[i] = inv * raw[i];
-   // up to 8192 columns: var (8 B) + flags (4 B) per column
+   float f32[9];
+   for (int i = 0; i < 9; ++i) {
+      f[i] = inv * raw[i];
+      f32[i] = (float)f[i];
+   }
+   // up to 8192 columns: var (8 B), var32 (4 B) and flags (4 B) per column
    cudaError_t e = cudaFuncSetAttribute(defect_flags, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        8192 * 12 + 64);
+                                        8192 * 16 + 64);
    if (e != cudaSuccess) return e;
-   return cudaMemcpyToSymbolAsync(c_defect_filter, f, sizeof(f), 0, cudaMemcpyHostToDevice, st);
+   e = cudaMemcpyToSymbolAsync(c_defect_filter, f, sizeof(f), 0, cudaMemcpyHostToDevice, st);
+   if (e != cudaSuccess) return e;
+   return cudaMemcpyToSymbolAsync(c_defect_filter32, f32, sizeof(f32), 0, cudaMemcpyHostToDevice, st);
 }
 
 cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const DefectCfg& cfg,
@@ -367,7 +416,7 @@ cudaError_t launch_defect_detect(const uint16_t* frames, int batch, const Defect
                 batch);
       defect_stats<<<grid, kStatThreads, 0, st>>>(frames, ws.stats, cfg.P, cfg.D, cfg.modules);
    }
-   const size_t smem = sizeof(double) * cfg.D + sizeof(int) * (cfg.D + 1);
+   const size_t smem = sizeof(double) * cfg.D + sizeof(float) * cfg.D + sizeof(int) * (cfg.D + 1);
    defect_flags<<<batch, 256, smem, st>>>(ws.stats, cfg, flags_out, ws.counts, ws.runs, ws.fix_counts,
                                           ws.fixes);
    return cudaGetLastError();

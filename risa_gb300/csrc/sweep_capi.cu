@@ -244,6 +244,30 @@ risa_gb_status risa_gb_sweep_enqueue(risa_gb_sweep* h, const uint16_t* raw, floa
    return RISA_GB_OK;
 }
 
+risa_gb_status risa_gb_sweep_graph_capture(risa_gb_sweep* h, const uint16_t* raw, float* img, void* stream,
+                                          risa_gb_graph** out) {
+   if (!h || !raw || !img || !out) return fail(RISA_GB_EINVAL, "null handle, buffer or output");
+   if (!stream) return fail(RISA_GB_EINVAL, "graph capture needs a non-default stream");
+   *out = nullptr;
+   std::unique_ptr<risa_gb_graph> gr(new (std::nothrow) risa_gb_graph());
+   if (!gr) return fail(RISA_GB_ENOMEM, "host allocation failed");
+   cudaStream_t st = static_cast<cudaStream_t>(stream);
+   cudaGraph_t graph = nullptr;
+   RG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+   const risa_gb_status s = risa_gb_sweep_enqueue(h, raw, img, stream);
+   const cudaError_t e = cudaStreamEndCapture(st, &graph);
+   if (s != RISA_GB_OK || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return s != RISA_GB_OK ? s : fail(RISA_GB_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+   }
+   gr->kernels = 1;
+   const cudaError_t ei = cudaGraphInstantiate(&gr->exec, graph, 0);
+   cudaGraphDestroy(graph);
+   if (ei != cudaSuccess) return fail(RISA_GB_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+   *out = gr.release();
+   return RISA_GB_OK;
+}
+
 risa_gb_status risa_gb_sweep_times(risa_gb_sweep* h, uint64_t* first_ns, uint64_t* done_ns, uint64_t* launch_ns) {
    if (!h) return fail(RISA_GB_EINVAL, "null handle");
    RG_CUDA(cudaDeviceSynchronize());

@@ -65,6 +65,58 @@ def test_defects_bit_exact(golden_dir, quirk):
             np.testing.assert_array_equal(got[0], d[f"{name}_repaired"])
 
 
+def _column_var_and_threshold(frame, quirk):
+    """The reference's per-column variance and 17-tap threshold in FP64, in its
+    operation order (interpolationFunctions.h:36-57), separate roundings."""
+    x = frame.astype(np.int64)
+    P, D = x.shape
+    tv = np.abs(np.diff(x, axis=0)).sum(axis=0)
+    rng = x[:-1].max(axis=0) - x[:-1].min(axis=0)
+    var = [float(np.float64(tv[d]) * np.float64(rng[d] * rng[d])) for d in range(D)]
+    raw = [0.5, 1.0, 1.0, 1.0, 1.5, 2.0, 3.0, 3.5, 2.0, 3.5, 3.0, 2.0, 1.5, 1.0, 1.0, 1.0, 0.5]
+    tot = 0.0
+    for r in raw:
+        tot += r
+    inv = 1.0 / tot
+    f = [inv * raw[j] for j in range(9)]
+    H = D // 2
+    th = np.zeros(D)
+    for t in range(2 * H):
+        seg, i = divmod(t, H)
+        acc = 0.0
+        for j in range(9):
+            i1 = ((i - j) & 0xFFFFFFFF) % H if quirk == rg.QUIRKS_RISA else (i - j) % H
+            acc = acc + f[j] * var[i1 + seg * H]
+            acc = acc + f[j] * var[(i + j) % H + seg * H]
+        th[seg * H + i] = acc
+    return np.array(var), th
+
+
+@pytest.mark.parametrize("quirk", [rg.QUIRKS_RISA, rg.QUIRKS_NONE])
+def test_defect_thresholds_on_the_boundary(golden_dir, quirk):
+    """Thresholds set to var/th of chosen columns put those columns on the
+    comparison's boundary, where the FP32 screen of the flagging kernel cannot
+    decide and the FP64 sequence must; flags match the oracle bit for bit."""
+    frame = np.load(os.path.join(golden_dir, "defects.npz"))["mid_frame"]
+    P, D = frame.shape
+    var, th = _column_var_and_threshold(frame, quirk)
+    cols = [d for d in range(0, D, 37) if var[d] > 0 and th[d] > 0][:6]
+    assert len(cols) >= 4
+    g = rg.make_geometry(n_fan_det=D, n_fan_proj=P)
+    t = dev(np.stack([frame] * 2).view(np.int16))
+    for d in cols:
+        ratio = var[d] / th[d]
+        for tmin, tmax in ((ratio, 1e30), (1e-30, ratio), (np.nextafter(ratio, 0), np.nextafter(ratio, 2 * ratio))):
+            h = rg.Defects(g, rg.make_params(quirks=quirk, thresh_min=tmin, thresh_max=tmax), max_batch=2)
+            ws = torch.empty(h.workspace_bytes(2), dtype=torch.uint8, device="cuda")
+            flags = torch.zeros((2, D), dtype=torch.int32, device="cuda")
+            h.enqueue(t.clone(), 2, ws, flags_out=flags)
+            exp = oracle.find_defects(frame, tmin, tmax, quirk)[:D]
+            got = host(flags)
+            np.testing.assert_array_equal(got[0], exp, err_msg=f"column {d}, thresholds {tmin!r}, {tmax!r}")
+            np.testing.assert_array_equal(got[1], exp)
+
+
 def test_defects_on_scan_frames():
     sc = phantom.make_scan(2, 1, 200, 432, 215.0, 240.0, seed=3, defect_fraction=0.02, distinct=2)
     g = rg.make_geometry(n_fan_det=432, n_fan_proj=200)

@@ -98,3 +98,15 @@ def test_sweep_seeded_config_and_repeat():
     sw.enqueue(t_raw, t_img)
     sw.check()
     np.testing.assert_array_equal(t_img.cpu().numpy().view(np.uint32), img.view(np.uint32))
+    # the same launch captured as a CUDA graph and replayed twice
+    s = torch.cuda.Stream()
+    t_img.fill_(float("nan"))
+    graph = sw.graph_capture(t_raw, t_img, s)
+    for _ in range(2):
+        t_img.fill_(float("nan"))
+        graph.replay(s)
+        s.synchronize()
+        sw.check()
+        np.testing.assert_array_equal(t_img.cpu().numpy().view(np.uint32), img.view(np.uint32))
+    first, done, launch = sw.times()
+    assert (done >= first).all() and (first >= launch).all()
