@@ -231,7 +231,7 @@ struct risa_gb_backprojection {
    DevBuf pairs, err;
    DevBuf rowbase, colbase;  // adjoint: (hi, lo) line starts [Pp][N]
    DevBuf adj;               // adjoint: slice-interleaved image copies (reserve_adjoint)
-   DevBuf tile_win, tile_win64;  // staged variants: window start + origin per 32 / 64 tile and angle
+   DevBuf tile_win;          // staged variants: window start + origin per tile and angle
    std::vector<float> a_host, b_host;  // the staged variants' kernel-parameter copies of a and b
    BPCfg cfg(bool fused_mask) const {
       BPCfg c;
@@ -255,7 +255,6 @@ struct risa_gb_backprojection {
       c.rowbase = rowbase.as<float2>();
       c.colbase = colbase.as<float2>();
       c.tile_win = tile_win.as<int2>();
-      c.tile_win64 = tile_win64.as<int2>();
       c.adj_scratch = adj.p;
       c.adj_scratch_bytes = adj.bytes;
       return c;
@@ -805,12 +804,9 @@ risa_gb_status risa_gb_backprojection_create(const risa_gb_geometry* gi, const r
       // 8 B per tile and angle (2 MB for 512^2 x 1024 angles); very large
       // geometries keep computing the window starts on the device instead
       const size_t tiles = (size_t)((h->g.N + 31) / 32) * ((h->g.N + 31) / 32);
-      if (tiles * (size_t)h->g.Pp * sizeof(int2) <= ((size_t)256 << 20)) {
+      if (tiles * (size_t)h->g.Pp * sizeof(int2) <= ((size_t)256 << 20))
          RG_TRY(h->tile_win.upload(bp_tile_windows(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(), t.t0.data(),
-                                                   h->g.Pp, h->g.N, 32)));
-         RG_TRY(h->tile_win64.upload(bp_tile_windows(t.a.data(), t.b.data(), t.ad.data(), t.bd.data(),
-                                                     t.t0.data(), h->g.Pp, h->g.N, 64)));
-      }
+                                                   h->g.Pp, h->g.N)));
       RG_TRY(h->rowbase.upload(bp_line_starts(t.t0.data(), t.bd.data(), h->g.Pp, h->g.N)));
       RG_TRY(h->colbase.upload(bp_line_starts(t.t0.data(), t.ad.data(), h->g.Pp, h->g.N)));
    }

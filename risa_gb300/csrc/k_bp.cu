@@ -33,7 +33,6 @@ struct BPVariant {
    int kind, slices, achunk, ppt;  // ppt: pixels per thread of the staged kernels
    const char* name;
    bool cp = false;  // staged: angle coefficients from the constant bank (at most kCPAngles angles)
-   int tile = 32;    // staged: pixel tile side (32: 256 threads; 64: 1024 threads, half the window bytes per update)
 };
 constexpr BPVariant kVariants[] = {
     {kPairs, 2, 32, 4, "pairs_s2_a32"},
@@ -58,8 +57,6 @@ constexpr BPVariant kVariants[] = {
     {kAsync, 4, 8, 4, "staged_cp_s4_a8_p4", true},
     {kAsync, 4, 16, 4, "staged_cp_s4_a16_p4", true},
     {kAsync, 2, 16, 4, "staged_cp_s2_a16_p4", true},
-    {kAsync, 4, 8, 4, "staged_cp_t64_s4_a8_p4", true, 64},
-    {kAsync, 4, 4, 4, "staged_cp_t64_s4_a4_p4", true, 64},
 };
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -402,11 +399,11 @@ cudaError_t launch_pairs_fit(const float* sino, float* img, int batch, const BPC
 // Window start (bin of window entry 0) of tile origin (x0, y0) for angle
 // `ang`; the host mirrors this exactly to size the padding.
 __device__ __forceinline__ int tile_window_start(const BPCfg& cfg, int ang, int x0, int y0, float a, float b,
-                                                 double* base_out, float span = 31.f) {
+                                                 double* base_out) {
    const double base = __dadd_rn(__dadd_rn(__ldg(cfg.t0 + ang), __dmul_rn((double)x0, __ldg(cfg.ad + ang))),
                                  __dmul_rn((double)y0, __ldg(cfg.bd + ang)));
-   const double tmin = __dadd_rn(__dadd_rn(base, (double)fminf(0.f, __fmul_rn(span, a))),
-                                 (double)fminf(0.f, __fmul_rn(span, b)));
+   const double tmin = __dadd_rn(__dadd_rn(base, (double)fminf(0.f, __fmul_rn(31.f, a))),
+                                 (double)fminf(0.f, __fmul_rn(31.f, b)));
    *base_out = base;
    return (int)floor(tmin) - 2;
 }
@@ -474,18 +471,13 @@ struct BPAngleParams {
 };
 struct BPNoAngleParams {};
 
-// T: pixel tile side (32 or 64). A warp covers an 8 x 4 pixel block per step;
-// the T/8 warps of a row of blocks lie side by side, RS rows apart step to step.
-template <int S, int ACH, bool PACKED, int PPT, int NST, bool CP, int T>
-__global__ void __launch_bounds__(T * T / PPT)
+template <int S, int ACH, bool PACKED, int PPT, int NST, bool CP>
+__global__ void __launch_bounds__(1024 / PPT)
     bp_linear_async(const float4* __restrict__ pairs, float* __restrict__ img, BPCfg cfg, int wlen, int batch,
                     const __grid_constant__ std::conditional_t<CP, BPAngleParams, BPNoAngleParams> ap) {
    static_assert(NST >= 2 && NST <= 4, "2 to 4 stages (one named barrier each)");
    static_assert(!CP || ACH % 4 == 0, "window coordinates are read four angles at a time");
-   static_assert(T == 32 || T == 64, "32 or 64 pixel tiles");
-   constexpr int H = S / 2, NT = T * T / PPT, WX = T / 8;
-   constexpr int RS = (NT / 32 / WX) * 4;  // rows between a thread's pixels
-   static_assert(RS * PPT == T && NT <= 1024, "the tile's warps cover it in PPT steps");
+   constexpr int T = 32, H = S / 2, NT = 1024 / PPT, RS = NT / 32;  // RS: rows between a thread's pixels
    extern __shared__ float4 wsm[];  // [NST][ACH][H][wlen]
    __shared__ uint64_t full[NST];
    // per angle of a chunk: (a, b, window-relative coordinate, unused), read
@@ -501,8 +493,8 @@ __global__ void __launch_bounds__(T * T / PPT)
    const int g = blockIdx.z, s0 = g * S;
    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
    // 8 x 4 pixels per warp, lanes 8i..8i+7 on a 4 x 2 block
-   const int xo = (warp % WX) * 8 + (lane & 3) + ((lane >> 1) & 4);
-   const int yo = (warp / WX) * 4 + ((lane >> 2) & 1) + ((lane >> 3) & 2);
+   const int xo = (warp & 3) * 8 + (lane & 3) + ((lane >> 1) & 4);
+   const int yo = (warp >> 2) * 4 + ((lane >> 2) & 1) + ((lane >> 3) & 2);
    const float c = 0.5f * (float)(N - 1);
    const float lim = (float)N * (float)N * 0.25f;
 
@@ -546,14 +538,13 @@ __global__ void __launch_bounds__(T * T / PPT)
          const float a = __ldg(cfg.a + ang), b = __ldg(cfg.b + ang);
          int w0;
          float rel;
-         const int2* twin = T == 64 ? cfg.tile_win64 : cfg.tile_win;
-         if (twin) {  // the host's table of the same FP64 arithmetic
-            const int2 e = __ldg(twin + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * Pp + ang);
+         if (cfg.tile_win) {  // the host's table of the same FP64 arithmetic
+            const int2 e = __ldg(cfg.tile_win + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * Pp + ang);
             w0 = e.x;
             rel = __int_as_float(e.y);
          } else {
             double base;
-            w0 = tile_window_start(cfg, ang, x0, y0, a, b, &base, (float)(T - 1));
+            w0 = tile_window_start(cfg, ang, x0, y0, a, b, &base);
             rel = (float)(base - (double)w0 - 0.5);
          }
          int u0 = w0 + cfg.win_lo;
@@ -618,11 +609,11 @@ __global__ void __launch_bounds__(T * T / PPT)
    unsigned live = (1u << PPT) - 1u;
    if (cfg.masking) {
       live = 0u;
-      const int xa = x0 + (warp % WX) * 8;
+      const int xa = x0 + (warp & 3) * 8;
       const float nx = fminf(fmaxf(c, (float)xa), (float)(xa + 7)) - c;
 #pragma unroll
       for (int r = 0; r < PPT; ++r) {
-         const int ya = y0 + (warp / WX) * 4 + RS * r;
+         const int ya = y0 + (warp >> 2) * 4 + RS * r;
          const float ny = fminf(fmaxf(c, (float)ya), (float)(ya + 3)) - c;
          if (nx * nx + ny * ny <= lim) live |= 1u << r;
       }
@@ -758,10 +749,10 @@ inline size_t async_smem(int S, int ach, int wlen, int nst = 2) {
    return (size_t)nst * sizeof(float2) * (size_t)S * ach * wlen;
 }
 
-template <int S, int ACH, bool PACKED, int PPT, int NST = 2, bool CP = false, int T = 32>
+template <int S, int ACH, bool PACKED, int PPT, int NST = 2, bool CP = false>
 cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& cfg, cudaStream_t st) {
    if (CP && (cfg.Pp > kCPAngles || !cfg.a_host || !cfg.b_host)) return cudaErrorInvalidConfiguration;
-   const int wlen = window_len(cfg.scale, T, T);
+   const int wlen = window_len(cfg.scale, 32, 32);
    const size_t smem = async_smem(S, ACH, wlen, NST);
    if (smem > kMaxPairsSmem) return cudaErrorInvalidConfiguration;
    // transaction bytes armed on one mbarrier phase stay below 2^20
@@ -777,35 +768,31 @@ cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& 
       if (e != cudaSuccess) return e;
    }
    if (cfg.mid_event && (e = cudaEventRecord(cfg.mid_event, st)) != cudaSuccess) return e;
-   auto kern = bp_linear_async<S, ACH, PACKED, PPT, NST, CP, T>;
+   auto kern = bp_linear_async<S, ACH, PACKED, PPT, NST, CP>;
    if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
    }
-   dim3 grid((cfg.N + T - 1) / T, (cfg.N + T - 1) / T, groups);
+   dim3 grid((cfg.N + 31) / 32, (cfg.N + 31) / 32, groups);
    std::conditional_t<CP, BPAngleParams, BPNoAngleParams> ap{};
    if constexpr (CP) {
       std::memcpy(ap.a, cfg.a_host, sizeof(float) * cfg.Pp);
       std::memcpy(ap.b, cfg.b_host, sizeof(float) * cfg.Pp);
    }
-   kern<<<grid, T * T / PPT, smem, st>>>(reinterpret_cast<const float4*>(cfg.pairs), img, cfg, wlen, batch, ap);
+   kern<<<grid, 1024 / PPT, smem, st>>>(reinterpret_cast<const float4*>(cfg.pairs), img, cfg, wlen, batch, ap);
    return cudaGetLastError();
 }
 
-template <int S, bool PACKED, int PPT, bool CP = false, int T = 32>
+template <int S, bool PACKED, int PPT, bool CP = false>
 cudaError_t launch_async_fit(const float* sino, float* img, int batch, const BPCfg& cfg, int ach,
                              cudaStream_t st) {
-   const int wlen = window_len(cfg.scale, T, T);
+   const int wlen = window_len(cfg.scale, 32, 32);
    while (ach > 4 && async_smem(S, ach, wlen) > kMaxPairsSmem) ach /= 2;
-   if (T == 64) {  // the 64-pixel tiles take angle chunks of 8 or 4
-      if (ach >= 8) return launch_async<S, 8, PACKED, PPT, 2, CP, T>(sino, img, batch, cfg, st);
-      return launch_async<S, 4, PACKED, PPT, 2, CP, T>(sino, img, batch, cfg, st);
-   }
    switch (ach) {
-      case 32: return launch_async<S, 32, PACKED, PPT, 2, CP, T>(sino, img, batch, cfg, st);
-      case 16: return launch_async<S, 16, PACKED, PPT, 2, CP, T>(sino, img, batch, cfg, st);
-      case 8: return launch_async<S, 8, PACKED, PPT, 2, CP, T>(sino, img, batch, cfg, st);
-      default: return launch_async<S, 4, PACKED, PPT, 2, CP, T>(sino, img, batch, cfg, st);
+      case 32: return launch_async<S, 32, PACKED, PPT, 2, CP>(sino, img, batch, cfg, st);
+      case 16: return launch_async<S, 16, PACKED, PPT, 2, CP>(sino, img, batch, cfg, st);
+      case 8: return launch_async<S, 8, PACKED, PPT, 2, CP>(sino, img, batch, cfg, st);
+      default: return launch_async<S, 4, PACKED, PPT, 2, CP>(sino, img, batch, cfg, st);
    }
 }
 
@@ -1026,30 +1013,27 @@ size_t bp_pairs_bytes(int variant, int batch, int Pp, int win_len) {
 
 void bp_window_extent(const float* a, const float* b, const double* ad, const double* bd, const double* t0,
                       int Pp, int N, float scale, bool masking, int* win_lo, int* win_len) {
-   // mirrors tile_window_start and the tile skip test of bp_linear_async for
-   // both tile sides (host code is compiled without floating-point contraction)
+   // mirrors tile_window_start and the tile skip test of bp_linear_async
+   // (host code is compiled without floating-point contraction)
+   const int wlen = window_len(scale, 32, 32);
+   const int tiles = (N + 31) / 32;
    const double c = 0.5 * (double)(N - 1), lim = (double)N * (double)N * 0.25;
    long lo = 0x7fffffff, hi = -0x7fffffff;
-   for (int T : {32, 64}) {
-      const int wlen = window_len(scale, T, T);
-      const int tiles = (N + T - 1) / T;
-      const float span = (float)(T - 1);
-      for (int by = 0; by < tiles; ++by) {
-         for (int bx = 0; bx < tiles; ++bx) {
-            const int x0 = bx * T, y0 = by * T;
-            if (masking) {
-               const double nx = std::fmin(std::fmax(c, (double)x0), (double)(x0 + T - 1)) - c;
-               const double ny = std::fmin(std::fmax(c, (double)y0), (double)(y0 + T - 1)) - c;
-               if (nx * nx + ny * ny > lim * (1.0 + 1e-6) + 1.0) continue;  // surely skipped
-            }
-            for (int i = 0; i < Pp; ++i) {
-               const double base = (t0[i] + (double)x0 * ad[i]) + (double)y0 * bd[i];
-               const float ma = span * a[i], mb = span * b[i];
-               const double tmin = (base + (double)std::fmin(0.f, ma)) + (double)std::fmin(0.f, mb);
-               const long w0 = (long)std::floor(tmin) - 2;
-               lo = std::min(lo, w0);
-               hi = std::max(hi, w0 + wlen);
-            }
+   for (int by = 0; by < tiles; ++by) {
+      for (int bx = 0; bx < tiles; ++bx) {
+         const int x0 = bx * 32, y0 = by * 32;
+         if (masking) {
+            const double nx = std::fmin(std::fmax(c, (double)x0), (double)(x0 + 31)) - c;
+            const double ny = std::fmin(std::fmax(c, (double)y0), (double)(y0 + 31)) - c;
+            if (nx * nx + ny * ny > lim * (1.0 + 1e-6) + 1.0) continue;  // surely skipped
+         }
+         for (int i = 0; i < Pp; ++i) {
+            const double base = (t0[i] + (double)x0 * ad[i]) + (double)y0 * bd[i];
+            const float ma = 31.f * a[i], mb = 31.f * b[i];
+            const double tmin = (base + (double)std::fmin(0.f, ma)) + (double)std::fmin(0.f, mb);
+            const long w0 = (long)std::floor(tmin) - 2;
+            lo = std::min(lo, w0);
+            hi = std::max(hi, w0 + wlen);
          }
       }
    }
@@ -1060,19 +1044,18 @@ void bp_window_extent(const float* a, const float* b, const double* ad, const do
 }
 
 std::vector<int2> bp_tile_windows(const float* a, const float* b, const double* ad, const double* bd,
-                                  const double* t0, int Pp, int N, int T) {
-   // tile_window_start of every T x T tile and angle, in the same rounded
+                                  const double* t0, int Pp, int N) {
+   // tile_window_start of every 32 x 32 tile and angle, in the same rounded
    // FP64 steps (host code is compiled without floating-point contraction)
-   const int tiles = (N + T - 1) / T;
-   const float span = (float)(T - 1);
+   const int tiles = (N + 31) / 32;
    std::vector<int2> out((size_t)tiles * tiles * Pp);
    for (int by = 0; by < tiles; ++by)
       for (int bx = 0; bx < tiles; ++bx) {
-         const int x0 = bx * T, y0 = by * T;
+         const int x0 = bx * 32, y0 = by * 32;
          int2* row = out.data() + ((size_t)by * tiles + bx) * Pp;
          for (int i = 0; i < Pp; ++i) {
             const double base = (t0[i] + (double)x0 * ad[i]) + (double)y0 * bd[i];
-            const float ma = span * a[i], mb = span * b[i];
+            const float ma = 31.f * a[i], mb = 31.f * b[i];
             const double tmin = (base + (double)std::fmin(0.f, ma)) + (double)std::fmin(0.f, mb);
             const int w0 = (int)std::floor(tmin) - 2;
             const float rel = (float)(base - (double)w0 - 0.5);
@@ -1111,7 +1094,6 @@ cudaError_t launch_backprojection(const float* sino, float* img, int batch, cons
    if (v.kind == kAsync || v.kind == kAsyncPacked) {
       const bool pk = v.kind == kAsyncPacked;
       const int ach = v.achunk;
-      if (v.cp && v.tile == 64) return launch_async_fit<4, false, 4, true, 64>(sino, img, batch, cfg, ach, st);
       if (v.cp)
          return v.slices == 2 ? launch_async_fit<2, false, 4, true>(sino, img, batch, cfg, ach, st)
                               : launch_async_fit<4, false, 4, true>(sino, img, batch, cfg, ach, st);

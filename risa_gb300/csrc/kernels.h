@@ -265,7 +265,6 @@ struct BPCfg {
    const float* b_host = nullptr;  // coefficients, at most kCPAngles angles)
    const int2* tile_win = nullptr;  // staged variants: per tile and angle (window start, bits of the float
                                     // coordinate of the tile origin in it), bp_tile_windows; else FP64 on device
-   const int2* tile_win64 = nullptr;  // the same for the 64 x 64 tiles
    void* adj_scratch = nullptr;  // adjoint: slice-interleaved image copies (bp_adjoint_scratch_bytes)
    size_t adj_scratch_bytes = 0;
    // adjoint: FP64 line starts split as (hi, lo) floats, [Pp][N]:
@@ -275,11 +274,11 @@ struct BPCfg {
 };
 // (hi, lo) float pairs of t0[i] + j * step[i], j < N, for every angle i.
 std::vector<float2> bp_line_starts(const double* t0, const double* step, int Pp, int N);
-// Window start and window-relative origin of every T x T tile and angle
+// Window start and window-relative origin of every 32 x 32 tile and angle
 // ([tile row][tile column][angle]), the staged kernels' FP64 window arithmetic
 // done once on the host.
 std::vector<int2> bp_tile_windows(const float* a, const float* b, const double* ad, const double* bd,
-                                  const double* t0, int Pp, int N, int T = 32);
+                                  const double* t0, int Pp, int N);
 int bp_variant_count();
 const char* bp_variant_name(int v);
 // Device bytes of the pair sinogram that `variant` needs for `batch` slices
