@@ -230,7 +230,11 @@ risa_gb_status risa_gb_fan2para_tables_host(const risa_gb_geometry* g, const ris
  * boxes one after the other with rows row_pitch entries apart. Arrays hold
  * L*tiles*16 and L*4*Pp*Dp entries. *stage_entries = the most entries of one
  * tile's boxes, 0 when the geometry is not staged (the engine then gathers
- * from global memory). */
+ * from global memory). A tile whose slots 2 and 3 (the mirrored 360-degree
+ * sample) repeat slots 1 and 0 bit for bit in every output -- the same line
+ * seen from the opposite side, as in full-circle NONE-mode geometries -- has
+ * boxes (0, 0, 0, -1) for slots 2 and 3 and rel 0 there: the engine stages
+ * and blends its slots 0 and 1 only, with the same result. */
 risa_gb_status risa_gb_fan2para_staged_tables_host(const risa_gb_geometry* g, const risa_gb_params* p,
                                                    int32_t* boxes, uint32_t* rel, int* stage_entries);
 

@@ -177,9 +177,12 @@ static risa_gb_status prepare_f2p_staged(risa_gb_fan2para* h) {
    // the gather table as uploaded by risa_gb_fan2para_create
    std::vector<uint32_t> pk(h->packed.bytes / sizeof(uint32_t));
    if (pk.empty()) return RISA_GB_OK;
+   std::vector<float> u(pk.size()), v(pk.size());
    RG_CUDA(cudaMemcpy(pk.data(), h->packed.p, h->packed.bytes, cudaMemcpyDeviceToHost));
+   RG_CUDA(cudaMemcpy(u.data(), h->u.p, sizeof(float) * u.size(), cudaMemcpyDeviceToHost));
+   RG_CUDA(cudaMemcpy(v.data(), h->v.p, sizeof(float) * v.size(), cudaMemcpyDeviceToHost));
    F2PStaged st;
-   build_f2p_staged(pk.data(), h->g.L, h->g.Pf, h->g.Df, h->g.Pp, h->g.Dp, &st);
+   build_f2p_staged(pk.data(), u.data(), v.data(), h->g.L, h->g.Pf, h->g.Df, h->g.Pp, h->g.Dp, &st);
    if (st.stage_entries <= 0) return RISA_GB_OK;
    RG_TRY(h->srel.upload(st.rel));
    RG_TRY(h->boxes.upload(st.boxes));
@@ -527,9 +530,14 @@ risa_gb_status risa_gb_fan2para_staged_tables_host(const risa_gb_geometry* gi, c
    std::vector<F2PGather> planes;
    RG_TRY(build_f2p_gather_all(g, p, &planes));
    std::vector<uint32_t> pk;
-   for (auto& t : planes) pk.insert(pk.end(), t.packed.begin(), t.packed.end());
+   std::vector<float> u, v;
+   for (auto& t : planes) {
+      pk.insert(pk.end(), t.packed.begin(), t.packed.end());
+      u.insert(u.end(), t.u.begin(), t.u.end());
+      v.insert(v.end(), t.v.begin(), t.v.end());
+   }
    F2PStaged st;
-   build_f2p_staged(pk.data(), g.L, g.Pf, g.Df, g.Pp, g.Dp, &st);
+   build_f2p_staged(pk.data(), u.data(), v.data(), g.L, g.Pf, g.Df, g.Pp, g.Dp, &st);
    *stage_entries = st.stage_entries;
    if (st.stage_entries > 0) {
       std::memcpy(boxes, st.boxes.data(), sizeof(int4) * st.boxes.size());

@@ -10,6 +10,7 @@
 // built in FP64 on the host). The table entries are loaded once and reused
 // for kFramesPerThread frames of the same plane.
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "async_copy.h"
@@ -228,6 +229,10 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
       b[s] = __ldg(bx + s);
       base[s + 1] = base[s] + b[s].z * f2p_box_pitch(b[s].w);
    }
+   // a mirrored tile (slots 2, 3 repeat slots 1, 0 in every output; boxes
+   // (0, 0, 0, -1) for them) stages and blends two slots: the fold
+   // 0.5 (sa (w0 + w1) + sa (w1 + w0)) is sa (w0 + w1), the same bits
+   const bool mirror = b[2].w < 0;
    int goff[kStageSlotsPerThread];
 #pragma unroll
    for (int i = 0; i < kStageSlotsPerThread; ++i) {
@@ -291,15 +296,24 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
       if (act) {
          const uint32_t sb = sbase + (uint32_t)(t & 1) * stage_bytes;
          ulonglong2 w[4];
+         unsigned long long r01, r23;
+         if (mirror) {
 #pragma unroll
-         for (int s = 0; s < 4; ++s)
-            w[s] = (rel[s] >> 31) ? bilinear4_smem(sb + (rel[s] & 0xFFFFu) * 16u, ((rel[s] >> 20) & 0xFFu) * 16u,
-                                                   u2[s], v2[s])
-                                  : make_ulonglong2(0ull, 0ull);
-         const unsigned long long r01 =
-             f2_mul(f2_add(f2_mul(f2_add(w[0].x, w[1].x), sa2), f2_mul(f2_add(w[2].x, w[3].x), sb2)), half2);
-         const unsigned long long r23 =
-             f2_mul(f2_add(f2_mul(f2_add(w[0].y, w[1].y), sa2), f2_mul(f2_add(w[2].y, w[3].y), sb2)), half2);
+            for (int s = 0; s < 2; ++s)
+               w[s] = (rel[s] >> 31) ? bilinear4_smem(sb + (rel[s] & 0xFFFFu) * 16u,
+                                                      ((rel[s] >> 20) & 0xFFu) * 16u, u2[s], v2[s])
+                                     : make_ulonglong2(0ull, 0ull);
+            r01 = f2_mul(f2_add(w[0].x, w[1].x), sa2);
+            r23 = f2_mul(f2_add(w[0].y, w[1].y), sa2);
+         } else {
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+               w[s] = (rel[s] >> 31) ? bilinear4_smem(sb + (rel[s] & 0xFFFFu) * 16u,
+                                                      ((rel[s] >> 20) & 0xFFu) * 16u, u2[s], v2[s])
+                                     : make_ulonglong2(0ull, 0ull);
+            r01 = f2_mul(f2_add(f2_mul(f2_add(w[0].x, w[1].x), sa2), f2_mul(f2_add(w[2].x, w[3].x), sb2)), half2);
+            r23 = f2_mul(f2_add(f2_mul(f2_add(w[0].y, w[1].y), sa2), f2_mul(f2_add(w[2].y, w[3].y), sb2)), half2);
+         }
          float r[4];
          f2_unpack(r01, r[0], r[1]);
          f2_unpack(r23, r[2], r[3]);
@@ -335,7 +349,8 @@ __global__ void __launch_bounds__(kThreads) fan2para_adjoint(const float* __rest
 }
 }  // namespace
 
-void build_f2p_staged(const uint32_t* packed, int L, int Pf, int Df, int Pp, int Dp, F2PStaged* out) {
+void build_f2p_staged(const uint32_t* packed, const float* u, const float* v, int L, int Pf, int Df, int Pp,
+                      int Dp, F2PStaged* out) {
    out->boxes.clear();
    out->rel.clear();
    out->stage_entries = 0;
@@ -360,14 +375,39 @@ void build_f2p_staged(const uint32_t* packed, int L, int Pf, int Df, int Pp, int
       *start = xs[(at + 1) % m];
       *len = m == n ? n + 1 : n - gap + 1;
    };
+   // Slots 2 and 3 (the mirrored 360-degree sample) equal slots 1 and 0 bit for
+   // bit -- index, validity and both weights -- in every output of the tile?
+   // In a full-circle geometry the mirrored sample (alpha + pi, -s) is the same
+   // line as (alpha, s), and its first ray is the other sample's second ray.
+   auto same_bits = [](float a, float b) { return std::memcmp(&a, &b, sizeof(float)) == 0; };
+   auto mirrored = [&](int k, int bt, int bs) {
+      if (!u || !v) return false;
+      const size_t b0 = (size_t)k * 4 * no;
+      for (int i = bt * kF2PTileAngles; i < std::min(Pp, (bt + 1) * kF2PTileAngles); ++i)
+         for (int j = bs * kF2PTileRays; j < std::min(Dp, (bs + 1) * kF2PTileRays); ++j) {
+            const size_t o = (size_t)i * Dp + j;
+            for (int s = 0; s < 2; ++s) {
+               const size_t a = b0 + (size_t)s * no + o, m = b0 + (size_t)(3 - s) * no + o;
+               if (packed[a] != packed[m] || !same_bits(u[a], u[m]) || !same_bits(v[a], v[m])) return false;
+            }
+         }
+      return true;
+   };
    int most = 0;
    std::vector<int> rows, cols;
    for (int k = 0; k < L; ++k)
       for (int bt = 0; bt < tiles_t; ++bt)
          for (int bs = 0; bs < tiles_s; ++bs) {
             const int tile = bt * tiles_s + bs;
+            // a mirrored tile stages and blends slots 0 and 1 only; its boxes
+            // of slots 2 and 3 are (0, 0, 0, -1), which marks it
+            const bool mirror = mirrored(k, bt, bs);
             int base = 0;
             for (int s = 0; s < 4; ++s) {
+               if (mirror && s >= 2) {
+                  boxes[((size_t)k * tiles + tile) * 4 + s] = make_int4(0, 0, 0, -1);
+                  continue;
+               }
                const uint32_t* pk = packed + ((size_t)k * 4 + s) * no;
                rows.clear();
                cols.clear();

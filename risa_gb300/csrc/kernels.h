@@ -185,7 +185,11 @@ struct F2PStaged {
 // From the gather tables ([L][4][Pp*Dp], bit 31 valid, bits 16..30 fan row,
 // bits 0..15 fan column). Leaves `out` empty when a tile's boxes exceed
 // kF2PMaxStageEntries.
-void build_f2p_staged(const uint32_t* packed, int L, int Pf, int Df, int Pp, int Dp, F2PStaged* out);
+// With the weights u, v (same layout), tiles whose slots 2 and 3 repeat slots 1
+// and 0 bit for bit in every output are staged with two slots (boxes of slots
+// 2 and 3 set to (0, 0, 0, -1)); u = v = nullptr stages four everywhere.
+void build_f2p_staged(const uint32_t* packed, const float* u, const float* v, int L, int Pf, int Df, int Pp,
+                      int Dp, F2PStaged* out);
 cudaError_t launch_fan2para(const float* fan, float* par, int batch, const F2PCfg& cfg,
                             cudaStream_t st);
 // Rebinning from frame quads (see QuadMap) into per-frame parallel sinograms.

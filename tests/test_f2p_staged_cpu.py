@@ -2,8 +2,10 @@
 valid output's four bilinear taps, followed through its tile's staged boxes
 the way the kernel stages them (entry -> box row and column -> fan row and
 column, both circular), land on the fan samples of the gather table; every
-tile's boxes fit the stage; geometries whose boxes are too large are left to
-the global-memory gather."""
+tile's boxes fit the stage; a tile marked mirrored (boxes (0, 0, 0, -1) for
+slots 2 and 3, staged and blended with two slots) has slots 2 and 3 equal to
+slots 1 and 0 bit for bit in every output; geometries whose boxes are too
+large are left to the global-memory gather."""
 import numpy as np
 import pytest
 
@@ -27,11 +29,21 @@ def check_staged(g, p):
     base = np.concatenate([np.zeros(boxes.shape[:2] + (1,), np.int64),
                            np.cumsum(boxes[..., 2] * pitches, axis=2)], axis=2)  # [L, tiles, 5]
     assert (base[..., 4] <= se).all()
+    mirror = (boxes[:, :, 2, 3] < 0) & (boxes[:, :, 3, 3] < 0)                 # [L, tiles]
+    assert ((boxes[:, :, 2:, 3] < 0) == mirror[..., None]).all()
     checked = 0
     for k in range(L):
-        pk = rg.fan2para_tables_host(g, p, k)[0]
+        pk, uu, vv = rg.fan2para_tables_host(g, p, k)
+        mo = mirror[k][tile]  # outputs of mirrored tiles
+        for s in (0, 1):
+            assert np.array_equal(pk[3 - s][mo], pk[s][mo])
+            assert np.array_equal(uu[3 - s][mo].view(np.uint32), uu[s][mo].view(np.uint32))
+            assert np.array_equal(vv[3 - s][mo].view(np.uint32), vv[s][mo].view(np.uint32))
         for s in range(4):
             valid = (pk[s] >> 31).astype(bool)
+            if s >= 2:
+                assert (rel[k, s][mo] == 0).all()
+                valid = valid & ~mo
             assert np.array_equal(valid, (rel[k, s] >> 31).astype(bool))
             o = np.flatnonzero(valid)
             tb = ((pk[s][o] >> 16) & 0x7FFF).astype(np.int64)
@@ -67,6 +79,17 @@ def test_staged_full_circle_boxes():
     ring, so the box holds one extra row or column for the +1 taps."""
     d = dict(SMALL, n_fan_proj=12, n_fan_det=16, n_par_proj=16, n_par_det=32, n_pixels=16)
     assert check_staged(geom(d), rg.make_params()) > 0
+
+
+def test_full_circle_tiles_are_mirrored():
+    """The full-rate streaming geometry (NONE mode): nearly every tile is
+    mirrored, RISA mode's reference steps break the symmetry."""
+    from tests.helpers import CFG2
+
+    none_boxes, _, se = rg.fan2para_staged_tables_host(geom(CFG2), rg.make_params())
+    assert se > 0 and (none_boxes[:, :, 2, 3] < 0).mean() > 0.99
+    risa_boxes, _, _ = rg.fan2para_staged_tables_host(geom(CFG2), rg.make_params(quirks=rg.QUIRKS_RISA))
+    assert (risa_boxes[:, :, 2, 3] < 0).mean() < 0.5
 
 
 def test_coarse_sampling_is_not_staged():
