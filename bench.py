@@ -383,7 +383,11 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     # the filter reads the rebinned sinogram; fused with the staging pass it
     # writes the padded pair records (8 B per window bin, angle and slice)
     win_lo, win_len = bp.window(True)
-    filt_bytes = B * ps * 4 + (B * Pp * win_len * 8 if t_stage < 1e-3 else B * ps * 4)
+    # with a staged variant the filter writes the pair records itself and no
+    # staging pass runs (its event interval is then only the events' own
+    # overhead, a few microseconds against ~1 ms for a real staging pass)
+    prefilled = t_stage < 0.05 * t_filt
+    filt_bytes = B * ps * 4 + (B * Pp * win_len * 8 if prefilled else B * ps * 4)
     yy, xx = np.mgrid[:N, :N]
     inside = int(((xx - (N - 1) / 2) ** 2 + (yy - (N - 1) / 2) ** 2 <= N * N / 4).sum())
     updates = B * inside * Pp
@@ -427,7 +431,9 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
         "fan2para": {"ms": t_f2p, "gbs": f2p_bytes / (t_f2p / 1e3) / 1e9,
                      "frac_hbm": f2p_bytes / (t_f2p / 1e3) / 1e9 / hbm},
         "filter": {"ms": t_filt, "gbs": filt_bytes / (t_filt / 1e3) / 1e9,
-                   "frac_hbm": filt_bytes / (t_filt / 1e3) / 1e9 / hbm},
+                   "frac_hbm": filt_bytes / (t_filt / 1e3) / 1e9 / hbm,
+                   "writes": "pair records, %d bins per angle and slice" % win_len if prefilled
+                             else "filtered sinogram"},
         "backprojection": {"ms": t_bp},
         "defect_detect": {"ms": t_def, "gbs": B * fs * 2 / (t_def / 1e3) / 1e9},
         "hbm_peak_gbs": hbm, "batch": B,

@@ -25,6 +25,16 @@ constexpr int kThreads = 256;
 // frame loop is fully unrolled so all their gathers are in flight together
 constexpr int kFramesPerThread = 8;
 
+// Slots 2 and 3 (the mirrored 360-degree sample) repeat slots 1 and 0 bit for
+// bit -- the same line seen from the other side, as in full-circle NONE-mode
+// tables: the fold 0.5 wa + 0.5 wb is then wa, and the mirrored taps need not
+// be read.
+__device__ __forceinline__ bool mirrored_slots(const uint32_t (&pk)[4], const float (&u)[4], const float (&v)[4]) {
+   return pk[2] == pk[1] && pk[3] == pk[0] && __float_as_uint(u[2]) == __float_as_uint(u[1]) &&
+          __float_as_uint(u[3]) == __float_as_uint(u[0]) && __float_as_uint(v[2]) == __float_as_uint(v[1]) &&
+          __float_as_uint(v[3]) == __float_as_uint(v[0]);
+}
+
 __device__ __forceinline__ float bilinear(const float* __restrict__ f, uint32_t pk, float u, float v,
                                           int Pf, int Df) {
    const int tb = (int)((pk >> 16) & 0x7FFFu), gb = (int)(pk & 0xFFFFu);
@@ -65,6 +75,7 @@ __global__ void __launch_bounds__(kThreads) fan2para_gather(const float* __restr
    }
    const int na = (int)(pk[0] >> 31) + (int)(pk[1] >> 31);
    const int nb = (int)(pk[2] >> 31) + (int)(pk[3] >> 31);
+   const bool mirror = mirrored_slots(pk, u, v);
    const size_t fs = (size_t)cfg.Pf * cfg.Df;
 #pragma unroll
    for (int m = 0; m < kFramesPerThread; ++m) {
@@ -74,11 +85,11 @@ __global__ void __launch_bounds__(kThreads) fan2para_gather(const float* __restr
       float w[4];
 #pragma unroll
       for (int s = 0; s < 4; ++s)
-         w[s] = (pk[s] >> 31) ? bilinear(fr, pk[s], u[s], v[s], cfg.Pf, cfg.Df) : 0.f;
+         w[s] = ((pk[s] >> 31) && (s < 2 || !mirror)) ? bilinear(fr, pk[s], u[s], v[s], cfg.Pf, cfg.Df) : 0.f;
       // per 360-degree sample: mean of its valid rays (r1/(r1+r2) weights)
       const float wa = na == 2 ? 0.5f * w[0] + 0.5f * w[1] : w[0] + w[1];
       const float wb = nb == 2 ? 0.5f * w[2] + 0.5f * w[3] : w[2] + w[3];
-      par[(size_t)f * no + o] = __fadd_rn(0.5f * wa, 0.5f * wb);
+      par[(size_t)f * no + o] = mirror ? wa : __fadd_rn(0.5f * wa, 0.5f * wb);
    }
 }
 
@@ -141,6 +152,7 @@ __global__ void __launch_bounds__(kThreads) fan2para_gather_quads(const float4* 
    }
    const int na = (int)(pk[0] >> 31) + (int)(pk[1] >> 31);
    const int nb = (int)(pk[2] >> 31) + (int)(pk[3] >> 31);
+   const bool mirror = mirrored_slots(pk, u, v);
    const size_t fs = (size_t)cfg.Pf * cfg.Df;
 #pragma unroll
    for (int t = 0; t < kQuadsPerThread; ++t) {
@@ -151,9 +163,13 @@ __global__ void __launch_bounds__(kThreads) fan2para_gather_quads(const float4* 
       float4 w[4];
 #pragma unroll
       for (int s = 0; s < 4; ++s)
-         w[s] = (pk[s] >> 31) ? bilinear4(fr, pk[s], u[s], v[s], cfg.Pf, cfg.Df) : make_float4(0.f, 0.f, 0.f, 0.f);
-      const float r[4] = {fold(w[0].x, w[1].x, w[2].x, w[3].x, na, nb), fold(w[0].y, w[1].y, w[2].y, w[3].y, na, nb),
-                          fold(w[0].z, w[1].z, w[2].z, w[3].z, na, nb), fold(w[0].w, w[1].w, w[2].w, w[3].w, na, nb)};
+         w[s] = ((pk[s] >> 31) && (s < 2 || !mirror)) ? bilinear4(fr, pk[s], u[s], v[s], cfg.Pf, cfg.Df)
+                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+      auto f1 = [&](float w0, float w1, float w2, float w3) {
+         return mirror ? (na == 2 ? 0.5f * w0 + 0.5f * w1 : w0 + w1) : fold(w0, w1, w2, w3, na, nb);
+      };
+      const float r[4] = {f1(w[0].x, w[1].x, w[2].x, w[3].x), f1(w[0].y, w[1].y, w[2].y, w[3].y),
+                          f1(w[0].z, w[1].z, w[2].z, w[3].z), f1(w[0].w, w[1].w, w[2].w, w[3].w)};
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
          const int b = quad_frame(qm, q, j);

@@ -105,6 +105,7 @@ def test_full_rate_streaming_configuration():
     # the autotuned variant (the benchmark's choice), enqueue and graph replay
     bp.set_variant(chosen)
     img.fill_(float("nan"))
+    torch.cuda.synchronize()  # the fill ran on the default stream, the engine runs on `stream`
     fbp.enqueue(raw, img, rg.PLANES_INTERLEAVED, n, stream)
     stream.synchronize()
     bp.check()
@@ -113,6 +114,7 @@ def test_full_rate_streaming_configuration():
     graph = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, stream)
     for _ in range(2):
         img.fill_(float("nan"))
+        torch.cuda.synchronize()
         graph.replay(stream)
         stream.synchronize()
         np.testing.assert_array_equal(img.cpu().numpy().view(np.uint32), direct.view(np.uint32))
@@ -124,6 +126,7 @@ def test_full_rate_streaming_configuration():
             continue
         bp.set_variant(v)
         img.fill_(float("nan"))
+        torch.cuda.synchronize()
         try:
             fbp.enqueue(raw, img, rg.PLANES_INTERLEAVED, n, stream)
         except rg.RisaError:

@@ -433,8 +433,9 @@ def test_graph_replay_and_host_path_match_enqueue():
     for c in range(0, n, B):
         fbp.enqueue(raw[c:c + B], ref_img[c:c + B], rg.PLANES_INTERLEAVED, B)
     expect = host(ref_img)
-    s = torch.cuda.Stream()
+    s = torch.cuda.Stream()  # not ordered with the default stream: synchronise at the hand-over
     img = torch.zeros((n, N, N), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
     graph = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, s)
     assert graph.kernel_count >= 2 * 5  # two chunks of the chain
     graph.replay(s)
@@ -483,6 +484,10 @@ def test_two_lanes_match_one_lane(variant):
             fbp.enqueue(raw[c:c + B], direct[c:c + B], rg.PLANES_INTERLEAVED, B)
         s = torch.cuda.Stream()
         img = torch.full((n, N, N), float("nan"), dtype=torch.float32, device="cuda")
+        # the enqueues and the fill ran on the default stream, which does not
+        # order torch's streams: the graph must not start before they finish
+        # (it uses the same engine buffers)
+        torch.cuda.synchronize()
         graph = fbp.graph_capture(raw, img, rg.PLANES_INTERLEAVED, n, s)
         for _ in range(2):
             graph.replay(s)

@@ -104,6 +104,7 @@ def test_sweep_seeded_config_and_repeat():
     graph = sw.graph_capture(t_raw, t_img, s)
     for _ in range(2):
         t_img.fill_(float("nan"))
+        torch.cuda.synchronize()  # the fill ran on the default stream
         graph.replay(s)
         s.synchronize()
         sw.check()
