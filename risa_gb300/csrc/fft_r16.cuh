@@ -106,6 +106,26 @@ __device__ __forceinline__ void dft16(float2* v) {
    for (int s = 0; s < 4; ++s) dft4(v[4 * s], v[4 * s + 1], v[4 * s + 2], v[4 * s + 3]);
 }
 
+// dft16 of a v whose v[8..15] are zero (the first pass of a row zero padded
+// to at least twice its length): each first-stage 4-point DFT has two zero
+// inputs and reduces to x0 +- x1, x0 +- (-i) x1; the rest is dft16's.
+__device__ __forceinline__ void dft16_lower_half(float2* v) {
+#pragma unroll
+   for (int q = 0; q < 4; ++q) {
+      const float2 x0 = v[q], x1 = v[q + 4], x1r = mul_mi(x1);
+      v[q] = cadd(x0, x1);
+      v[q + 4] = cadd(x0, x1r);
+      v[q + 8] = csub(x0, x1);
+      v[q + 12] = csub(x0, x1r);
+   }
+#pragma unroll
+   for (int q = 1; q < 4; ++q)
+#pragma unroll
+      for (int s = 1; s < 4; ++s) v[q + 4 * s] = w16(v[q + 4 * s], q * s);
+#pragma unroll
+   for (int s = 0; s < 4; ++s) dft4(v[4 * s], v[4 * s + 1], v[4 * s + 2], v[4 * s + 3]);
+}
+
 template <int R>
 __device__ __forceinline__ void dft_r(float2* v) {
    if (R == 16) dft16(v);
@@ -177,11 +197,13 @@ __device__ __forceinline__ int r16_time_index(int lt, int b, int r) {
 
 // Forward FFT of v (first pass's layout) through buf; on return v[b R3 + r]
 // holds the spectrum at index r16_time_index<LEN>(lt, b, r) and buf is free.
+// HALF: v[8..15] (time indices from LEN/2 on) are zero and need not be set.
 // All threads of the CTA must call it (CTA barriers inside).
-template <int LEN>
+template <int LEN, bool HALF = false>
 __device__ __forceinline__ void r16_forward(float2 (&v)[16], float2* buf, int lt, const float2* __restrict__ twp) {
    using P = R16Plan<LEN>;
-   r16_compute<LEN, 16, 1>(lt, v, nullptr);
+   if (HALF) dft16_lower_half(v);
+   else r16_compute<LEN, 16, 1>(lt, v, nullptr);
    r16_store<LEN, 16, 1>(buf, lt, v);
    __syncthreads();
    r16_load<LEN, P::R2>(buf, lt, v);
@@ -194,13 +216,13 @@ __device__ __forceinline__ void r16_forward(float2 (&v)[16], float2* buf, int lt
    r16_compute<LEN, P::R3, P::NS3>(lt, v, twp + P::TW3);
 }
 
-template <int LEN>
+template <int LEN, bool HALF = false>
 __device__ __forceinline__ void r16_filter_core(float2 (&v)[16], float2* buf, int lt, const float2* __restrict__ twp,
                                                 const float2* __restrict__ h, bool adjoint) {
    using P = R16Plan<LEN>;
    const float2* tw2 = twp;
    const float2* tw3 = twp + P::TW3;
-   r16_forward<LEN>(v, buf, lt, twp);
+   r16_forward<LEN, HALF>(v, buf, lt, twp);
    // Spectrum index of v[b R3 + r] is r16_time_index = lt + (LEN/16) m with
    // m = b + out_slot(r) (16/R3), and LEN = 16 R2 R3 makes m run over 0..15:
    // a thread holds exactly the 16 values the first inverse pass reads

@@ -325,10 +325,13 @@ cudaError_t launch_r16(float* sino, int total_rows, const FilterCfg& cfg, cudaSt
 //    pairs[g][angle][h][u] = (mid_2h, mid_2h+1, diff_2h, diff_2h+1),  k = u - win_lo,
 //    mid = (q[k] + q[k+1]) / 2, diff = q[k+1] - q[k], q = 0 outside the detector,
 // for every window bin u -- the filtered sinogram itself is never written.
-template <int LEN>
+// HALF (Dp <= LEN / 2, the rows zero padded to at least twice their length):
+// the upper half of the first pass's inputs is known to be zero, so it is
+// neither loaded nor transformed, and the outputs from LEN / 2 on, which no
+// record reads, are not formed.
+template <int LEN, bool HALF>
 __global__ void __launch_bounds__(r16_threads<LEN>(), 512 / r16_threads<LEN>())
-    filter_rows_r16_pairs(const float* __restrict__ sino, int batch,
-                                                                FilterCfg cfg, PairsOut po) {
+    filter_rows_r16_pairs(const float* __restrict__ sino, int batch, FilterCfg cfg, PairsOut po) {
    constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF, PL = LEN + LEN / 16;
    using P = R16Plan<LEN>;
    extern __shared__ float2 sm[];
@@ -343,44 +346,62 @@ __global__ void __launch_bounds__(r16_threads<LEN>(), 512 / r16_threads<LEN>())
    float2* buf = sm + local * PL;
    float2 v[16];
 #pragma unroll
-   for (int r = 0; r < 16; ++r) {
+   for (int r = 0; r < (HALF ? 8 : 16); ++r) {
       const int n = lt + r * TPF;
       v[r] = make_float2((has_a && n < Dp) ? row_a[n] : 0.f, (has_b && n < Dp) ? row_b[n] : 0.f);
    }
-   r16_filter_core<LEN>(v, buf, lt, cfg.twp, cfg.h, cfg.adjoint != 0);
+   r16_filter_core<LEN, HALF>(v, buf, lt, cfg.twp, cfg.h, cfg.adjoint != 0);
    __syncthreads();
+   // q[k] of both rows at qb[k + 1] (unpadded: the lanes of a warp store and
+   // load consecutive entries, whatever win_lo is), zero at k = -1 and k = Dp
+   float2* qb = buf;
 #pragma unroll
    for (int b = 0; b < 16 / P::R3; ++b)
 #pragma unroll
       for (int r = 0; r < P::R3; ++r) {
+         if (HALF && r >= P::R3 / 2) continue;  // time index LEN / 2 or more
          const int n = r16_time_index<LEN>(lt, b, r);
-         if (n < Dp) buf[pad16(n)] = make_float2(v[b * P::R3 + r].x, has_b ? -v[b * P::R3 + r].y : 0.f);
+         if (n < Dp) qb[n + 1] = make_float2(v[b * P::R3 + r].x, has_b ? -v[b * P::R3 + r].y : 0.f);
       }
+   if (lt == 0) {
+      qb[0] = make_float2(0.f, 0.f);
+      qb[Dp + 1] = make_float2(0.f, 0.f);
+   }
    __syncthreads();
    if (!has_a) return;
    const int g = s0 / po.S, h = (s0 % po.S) >> 1;
    float4* out = reinterpret_cast<float4*>(po.pairs) + (((size_t)g * Pp + ang) * (po.S / 2) + h) * po.wp;
    for (int u = lt; u < po.wp; u += TPF) {
       const int k = u - po.win_lo;
-      const float2 q0 = (k >= 0 && k < Dp) ? buf[pad16(k)] : make_float2(0.f, 0.f);
-      const float2 q1 = (k + 1 >= 0 && k + 1 < Dp) ? buf[pad16(k + 1)] : make_float2(0.f, 0.f);
-      out[u] = make_float4(0.5f * (q0.x + q1.x), 0.5f * (q0.y + q1.y), q1.x - q0.x, q1.y - q0.y);
+      float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (k >= -1 && k < Dp) {
+         const float2 q0 = qb[k + 1], q1 = qb[k + 2];
+         rec = make_float4(0.5f * (q0.x + q1.x), 0.5f * (q0.y + q1.y), q1.x - q0.x, q1.y - q0.y);
+      }
+      out[u] = rec;
    }
+}
+
+template <int LEN, bool HALF>
+cudaError_t launch_r16_pairs_as(const float* sino, int batch, const FilterCfg& cfg, const PairsOut& po,
+                                cudaStream_t st) {
+   constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF;
+   const size_t smem = sizeof(float2) * (size_t)FPB * (LEN + LEN / 16);
+   if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(filter_rows_r16_pairs<LEN, HALF>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+   }
+   const int pairs = (batch + 1) / 2 * cfg.rows;
+   filter_rows_r16_pairs<LEN, HALF><<<(pairs + FPB - 1) / FPB, r16_threads<LEN>(), smem, st>>>(sino, batch, cfg, po);
+   return cudaGetLastError();
 }
 
 template <int LEN>
 cudaError_t launch_r16_pairs(const float* sino, int batch, const FilterCfg& cfg, const PairsOut& po,
                              cudaStream_t st) {
-   constexpr int TPF = LEN / 16, FPB = r16_threads<LEN>() / TPF;
-   const size_t smem = sizeof(float2) * (size_t)FPB * (LEN + LEN / 16);
-   if (smem > 48 * 1024) {
-      cudaError_t e =
-          cudaFuncSetAttribute(filter_rows_r16_pairs<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-   }
-   const int pairs = (batch + 1) / 2 * cfg.rows;
-   filter_rows_r16_pairs<LEN><<<(pairs + FPB - 1) / FPB, r16_threads<LEN>(), smem, st>>>(sino, batch, cfg, po);
-   return cudaGetLastError();
+   return 2 * cfg.Dp <= LEN ? launch_r16_pairs_as<LEN, true>(sino, batch, cfg, po, st)
+                            : launch_r16_pairs_as<LEN, false>(sino, batch, cfg, po, st);
 }
 
 // One CTA: invert the summed (conjugated) spectrum, scale by 1/len, map lags to taps.
