@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(r16_threads<LEN>(), 512 / r16_threads<LEN>())
    for (int b = 0; b < 16 / P::R3; ++b)
 #pragma unroll
       for (int r = 0; r < P::R3; ++r) {
-         if (HALF && r >= P::R3 / 2) continue;  // time index LEN / 2 or more
+         if (HALF && out_slot<P::R3>(r) >= P::R3 / 2) continue;  // time index LEN / 2 or more
          const int n = r16_time_index<LEN>(lt, b, r);
          if (n < Dp) qb[n + 1] = make_float2(v[b * P::R3 + r].x, has_b ? -v[b * P::R3 + r].y : 0.f);
       }

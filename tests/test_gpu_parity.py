@@ -389,6 +389,42 @@ def test_fbp_long_filter_rows():
             assert mr < MAX_REL and l2 < MAX_REL, (plane, len(idx), b, mr, l2)
 
 
+@pytest.mark.parametrize("dp,pad,n_pix", [
+    (200, 512, 64),     # rows at most half the FFT length: the pass skips the zero half; one warp per row pair
+    (256, 512, 96),     # exactly half
+    (300, 512, 96),     # more than half: the general pass
+    (600, 1024, 128),   # general pass, two warps per row pair
+    (600, 0, 128),      # default padding (2048), four warps per row pair
+    (1500, 0, 128),     # 4096, eight warps per row pair
+])
+def test_fbp_filter_lengths(dp, pad, n_pix):
+    """The engine's filter pass writing the backprojection's pair records, at
+    every radix-16 length, with rows at most half, exactly half and more than
+    half the FFT length, an odd batch (the last pair without its second
+    slice), against the FP64 oracle."""
+    d, sc, g, p, op = _fbp_case(rg.QUIRKS_NONE, True, masking=True, L=2, frames=3)
+    d.update(n_par_proj=64, n_par_det=dp, n_pixels=n_pix)
+    g = geom(d)
+    p = rg.make_params(filter_type="sheppLogan", defects=True, masking=True, pad=pad)
+    op = oracle.make_params(quirk=oracle.QUIRK_NONE, filter_type="sheppLogan", defects=True, masking=True, pad=pad)
+    n = sc.raw.shape[0] - 1  # 5 frames
+    oref, odark = oracle.attenuation_init(sc.ref, sc.dark, 2, 0.67, 1.5, True, rg.QUIRKS_NONE)
+    rec = oracle.f2p_records(ns(d), rg.QUIRKS_NONE)
+    exp = oracle.fbp(ns(d), op, rec, oref, odark, sc.raw[:n], sc.planes[:n])
+    fbp = rg.FBP(g, p, sc.ref, 1, sc.dark, 1, max_batch=n)
+    names = [rg.Backprojection.variant_name(v) for v in range(rg.Backprojection.variant_count())]
+    raw = dev(sc.raw[:n].view(np.int16))
+    for variant in ("staged_cp_s4_a8_p4", "staged_s2_a16_p4"):  # 4 and 2 slices per pair-record group
+        fbp.backprojection().set_variant(names.index(variant))
+        img = torch.full((n, n_pix, n_pix), float("nan"), dtype=torch.float32, device="cuda")
+        fbp.enqueue(raw, img, rg.PLANES_INTERLEAVED, n)
+        got = host(img)
+        for b in range(n):
+            mr, l2 = rel_err(got[b], exp[b])
+            assert mr < MAX_REL and l2 < MAX_REL, (variant, b, mr, l2)
+    fbp.backprojection().check()
+
+
 def test_fbp_fused_filter_staging():
     """Staged backprojection variants with a radix-16 filter length: the filter
     writes the pair records itself (no staging pass); an odd batch leaves the
