@@ -682,7 +682,18 @@ __global__ void __launch_bounds__(1024 / PPT)
             if (a4 + 2 < na) angle(a4 + 2, make_float4(ap.a[ang + 2], ap.b[ang + 2], r4.z, 0.f), check);
             if (a4 + 3 < na) angle(a4 + 3, make_float4(ap.a[ang + 3], ap.b[ang + 3], r4.w, 0.f), check);
          };
-         if (live == (1u << PPT) - 1u) {
+         if (live == (1u << PPT) - 1u && na == ACH) {
+            // a whole chunk: four angles per step, none of them past the end
+#pragma unroll 1
+            for (int a4 = 0; a4 < ACH; a4 += 4) {
+               const float4 r4 = s_par[st][a4 >> 2];
+               const int ang = ch * ACH + a4;
+               angle(a4, make_float4(ap.a[ang], ap.b[ang], r4.x, 0.f), std::false_type{});
+               angle(a4 + 1, make_float4(ap.a[ang + 1], ap.b[ang + 1], r4.y, 0.f), std::false_type{});
+               angle(a4 + 2, make_float4(ap.a[ang + 2], ap.b[ang + 2], r4.z, 0.f), std::false_type{});
+               angle(a4 + 3, make_float4(ap.a[ang + 3], ap.b[ang + 3], r4.w, 0.f), std::false_type{});
+            }
+         } else if (live == (1u << PPT) - 1u) {
             for (int a4 = 0; a4 < na; a4 += 4) quad(a4, std::false_type{});
          } else {
             for (int a4 = 0; a4 < na; a4 += 4) quad(a4, std::true_type{});
