@@ -45,7 +45,7 @@ SMEM_BYTES_PER_CLK_SM = 128  # nominal shared-memory bandwidth per SM
 # backprojection variant (staged_cp_s4_a8_p4, profiles/bp_staged_fbp512_ncu.txt):
 # the pair records read once and the images written, both proportional to the
 # slices, so a launch of B slices moves B/64 of it
-BP_DRAM_BYTES_PER_SLICE = 727.8e6 / 64
+BP_DRAM_BYTES_PER_SLICE = 722.1e6 / 64
 WORKLOAD_NAME = ("full-rate streaming: 2 planes x 2000 frames of 1000x1152 uint16 fan sinograms, 1% defective "
                  "detectors -> 1024x1024 parallel (pad 2048, Shepp-Logan) -> 512^2 FP32, circular mask")
 
