@@ -456,11 +456,15 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     out["graph_overhead"] = {"sum_of_stage_ms_per_step": sum(es.values()) * chunks,
                              "chunks_per_step": chunks}
 
-    # ---- plain per-stage path: one frame per launch, sync after every stage
+    # ---- plain per-stage path: one frame per launch, sync after every stage;
+    # the backprojection variant autotuned for one slice per launch
     dfx = rg.Defects(g, p, max_batch=1)
     ws = torch.empty(dfx.workspace_bytes(1), dtype=torch.uint8, device=dev)
     raw1 = torch.empty((1, Pf, Df), dtype=torch.int16, device=dev)
     n_plain = min(64, n)
+    bp1 = rg.Backprojection(g, p)
+    bp1.reserve(1)
+    bp1_variant = bp1.autotune(par_buf, img.data_ptr(), 1, stream)
 
     def plain():
         for f in range(n_plain):
@@ -474,7 +478,7 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
             stream.synchronize()
             filt.enqueue(par_buf, 1, stream)
             stream.synchronize()
-            bp.enqueue(par_buf, img[f:f + 1], 1, stream)
+            bp1.enqueue(par_buf, img[f:f + 1], 1, stream)
             stream.synchronize()
 
     with torch.cuda.stream(stream):
@@ -485,7 +489,8 @@ def measure_extras(args, sc, fbp, raw, img, stream, B, variant, torch, rg, g, p)
     plain_value = n_plain / t_plain
     out["plain"] = {"value": plain_value, "unit": "slices/s", "frames": n_plain,
                     "how": "this library's stage kernels, one frame per stage launch, stream sync after each "
-                           "stage, device-resident input"}
+                           "stage, device-resident input",
+                    "bp_variant": rg.Backprojection.variant_name(bp1_variant)}
     try:
         out["plain_reference"] = measure_plain_reference(torch, rg, sc, raw, g, stream, min(32, n))
     except Exception as e:  # reported, never hides the headline line
