@@ -271,8 +271,10 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
    const size_t fs = (size_t)cfg.Pf * cfg.Df;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(stg);
    const uint32_t stage_bytes = (uint32_t)cfg.stage_entries * 16u;
+   // this thread's staging sources advance by one frame quad per quad
+   const float4* src_q = fanq + (size_t)(k * qm.per_plane + first) * fs;
    auto stage = [&](int t) {
-      const float4* src = fanq + (size_t)(k * qm.per_plane + first + t) * fs;
+      const float4* src = src_q + (size_t)t * fs;
       const uint32_t dst = sbase + (uint32_t)(t & 1) * stage_bytes + threadIdx.x * 16u;
 #pragma unroll
       for (int i = 0; i < kStageSlotsPerThread; ++i)
@@ -298,8 +300,14 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
    const float sa = (rel[0] >> 31) + (rel[1] >> 31) == 2 ? 0.5f : 1.f;
    const float sb = (rel[2] >> 31) + (rel[3] >> 31) == 2 ? 0.5f : 1.f;
    const unsigned long long sa2 = f2_pack(sa, sa), sb2 = f2_pack(sb, sb), half2 = f2_pack(0.5f, 0.5f);
-   // frames of quad (plane, local): b0 + stride * j
+   // frames of quad (plane, local): b0 + stride * j; the quad's 4 outputs
+   // at out_q + j * fstep, out_q advancing by 4 frames per quad
    const int stride = qm.plane >= 0 ? 1 : qm.L;
+   const int b_first = qm.plane >= 0 ? 4 * first : k + qm.L * 4 * first;
+   const size_t fstep = (size_t)stride * no;
+   float* out_q = par + (size_t)b_first * no + o;
+   // quads before this one hold 4 frames of the batch each
+   const int full_quads = (qm.batch - b_first - 3 * stride + 4 * stride - 1) / (4 * stride);
 
    for (int t = 0; t < nq; ++t) {
       if (t + 1 < nq) {
@@ -333,12 +341,15 @@ __global__ void __launch_bounds__(kStageThreads) fan2para_staged(const float4* _
          float r[4];
          f2_unpack(r01, r[0], r[1]);
          f2_unpack(r23, r[2], r[3]);
-         const int local = first + t;
-         const int b0 = qm.plane >= 0 ? 4 * local : k + qm.L * 4 * local;
+         float* out = out_q + (size_t)t * 4 * fstep;
+         if (t < full_quads) {  // all 4 frames of the quad are in the batch
 #pragma unroll
-         for (int j = 0; j < 4; ++j) {
-            const int bf = b0 + stride * j;
-            if (bf < qm.batch) par[(size_t)bf * no + o] = r[j];
+            for (int j = 0; j < 4; ++j) out[j * fstep] = r[j];
+         } else {
+            const int b0 = b_first + 4 * stride * t;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+               if (b0 + stride * j < qm.batch) out[j * fstep] = r[j];
          }
       }
       __syncthreads();  // stage t & 1 is refilled with quad t + 2 next
