@@ -140,13 +140,20 @@ __device__ __forceinline__ constexpr int out_slot(int i) {
    return R == 16 ? (i >> 2) + 4 * (i & 3) : i;
 }
 
+// pad16(x + c) = pad16(x) + c + c/16 for c a multiple of 16: the thread's
+// base address is formed once and every entry is a constant offset from it.
 template <int LEN, int R>
 __device__ __forceinline__ void r16_load(const float2* buf, int lt, float2 (&v)[16]) {
    constexpr int TPF = LEN / 16, NB = LEN / R;
+   static_assert(TPF % 16 == 0 && NB % 16 == 0, "offsets are multiples of 16");
+   const float2* p = buf + pad16(lt);
 #pragma unroll
    for (int b = 0; b < 16 / R; ++b)
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[b * R + r] = buf[pad16(lt + b * TPF + r * NB)];
+      for (int r = 0; r < R; ++r) {
+         const int c = b * TPF + r * NB;
+         v[b * R + r] = p[c + c / 16];
+      }
 }
 
 // Twiddles and butterflies of pass (R, NS); twp: that pass's table [R][NS].
@@ -164,15 +171,23 @@ __device__ __forceinline__ void r16_compute(int lt, float2 (&v)[16], const float
    }
 }
 
+// Output index d + out_slot(r) NS with d = (j - k) R + k, j = lt + b TPF,
+// k = j mod NS: for NS = 1 or 16 the slot term and the b term are multiples
+// of 16 above the low bits k, so pad16 splits as in r16_load.
 template <int LEN, int R, int NS>
 __device__ __forceinline__ void r16_store(float2* buf, int lt, const float2 (&v)[16]) {
    constexpr int TPF = LEN / 16;
+   static_assert(NS == 1 || NS == 16, "stores of the first two passes");
+   static_assert(NS == 16 || R == 16, "a first pass of radix 16");
+   const int k = lt & (NS - 1), d0 = (lt - k) * R + k;
+   float2* p = buf + pad16(d0);
 #pragma unroll
-   for (int b = 0; b < 16 / R; ++b) {
-      const int j = lt + b * TPF, k = j & (NS - 1), d = (j - k) * R + k;
+   for (int b = 0; b < 16 / R; ++b)
 #pragma unroll
-      for (int r = 0; r < R; ++r) buf[pad16(d + out_slot<R>(r) * NS)] = v[b * R + r];
-   }
+      for (int r = 0; r < R; ++r) {
+         const int c = b * TPF * R + out_slot<R>(r) * NS;  // a multiple of 16
+         p[c + c / 16] = v[b * R + r];
+      }
 }
 
 template <int LEN>
