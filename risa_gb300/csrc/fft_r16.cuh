@@ -39,7 +39,8 @@ __device__ __forceinline__ void dft2(float2* v) {
 
 __device__ __forceinline__ void dft4(float2& x0, float2& x1, float2& x2, float2& x3) {
    const float2 t0 = cadd(x0, x2), t1 = csub(x0, x2);
-   const float2 t2 = cadd(x1, x3), t3 = mul_mi(csub(x1, x3));
+   // (-i)(x1 - x3) as two scalar subtractions, formed in place as a pair
+   const float2 t2 = cadd(x1, x3), t3 = make_float2(x1.y - x3.y, x3.x - x1.x);
    x0 = cadd(t0, t2);
    x2 = csub(t0, t2);
    x1 = cadd(t1, t3);
