@@ -471,14 +471,16 @@ struct BPAngleParams {
 };
 struct BPNoAngleParams {};
 
-template <int S, int ACH, bool PACKED, int PPT, int NST, bool CP>
+template <int S, int ACH, bool PACKED, int PPT, int NST, bool CP, int WP = 0>
 __global__ void __launch_bounds__(1024 / PPT)
     bp_linear_async(const float4* __restrict__ pairs, float* __restrict__ img, BPCfg cfg, int wlen, int batch,
                     const __grid_constant__ std::conditional_t<CP, BPAngleParams, BPNoAngleParams> ap) {
    static_assert(NST >= 2 && NST <= 4, "2 to 4 stages (one named barrier each)");
    static_assert(!CP || ACH % 4 == 0, "window coordinates are read four angles at a time");
    constexpr int T = 32, H = S / 2, NT = 1024 / PPT, RS = NT / 32;  // RS: rows between a thread's pixels
-   extern __shared__ float4 wsm[];  // [NST][ACH][H][wlen]
+   // [NST][ACH][H][ws]: ws = WP entries (a compile-time stride, so the slice
+   // pairs of an entry are a constant offset apart) or wlen
+   extern __shared__ float4 wsm[];
    __shared__ uint64_t full[NST];
    // per angle of a chunk: (a, b, window-relative coordinate, unused), read
    // with one broadcast 16-byte load per angle (three 4-byte loads cost 8% of
@@ -518,7 +520,9 @@ __global__ void __launch_bounds__(1024 / PPT)
    const int nchunks = (Pp + ACH - 1) / ACH;
    const int wp = cfg.win_len;
    const float4* grow = pairs + (size_t)g * Pp * H * wp;
-   const uint32_t plane_bytes = (uint32_t)wlen * (uint32_t)sizeof(float4);
+   const uint32_t plane_bytes = (uint32_t)wlen * (uint32_t)sizeof(float4);  // one window copy
+   const int ws = WP > 0 ? WP : wlen;
+   const uint32_t stride_bytes = WP > 0 ? (uint32_t)WP * (uint32_t)sizeof(float4) : plane_bytes;
 
    // warp 0: parameters and bulk copies of chunk ch into stage st. The
    // parameters are stored before lane 0's arrive (a release), so a warp that
@@ -571,7 +575,7 @@ __global__ void __launch_bounds__(1024 / PPT)
          const int ang = ch * ACH + lane;
 #pragma unroll
          for (int h = 0; h < H; ++h)
-            async::bulk_load(wsm + ((size_t)(st * ACH + lane) * H + h) * wlen,
+            async::bulk_load(wsm + ((size_t)(st * ACH + lane) * H + h) * ws,
                              grow + ((size_t)ang * H + h) * wp + r.u0, plane_bytes, &full[st]);
       }
    };
@@ -623,7 +627,7 @@ __global__ void __launch_bounds__(1024 / PPT)
       const int st = ch % NST;
       if (!async::mbar_wait(&full[st], (uint32_t)((ch / NST) & 1), cfg.err, 5)) s_fail = 1;
       const int na = live ? min(ACH, Pp - ch * ACH) : 0;
-      const uint32_t sbase = wbase + (uint32_t)(st * ACH * H) * plane_bytes;
+      const uint32_t sbase = wbase + (uint32_t)(st * ACH * H) * stride_bytes;
       // one angle of the chunk; CHECK: skip the pixel steps whose block is
       // outside the circle (warp-uniform), otherwise straight-line code
       auto angle = [&](int ai, const float4 q, auto check) {
@@ -631,7 +635,7 @@ __global__ void __launch_bounds__(1024 / PPT)
          const float a = q.x, b = q.y;
          const float t0 = q.z + (float)xo * a + (float)yo * b;
          const float step = (float)RS * b;
-         const uint32_t abase = sbase + (uint32_t)(ai * H) * plane_bytes;
+         const uint32_t abase = sbase + (uint32_t)(ai * H) * stride_bytes;
          if (PACKED) {
             unsigned long long tm2 = f2_pack(t0, t0);
             const unsigned long long step2 = f2_pack(step, step);
@@ -646,7 +650,7 @@ __global__ void __launch_bounds__(1024 / PPT)
                   const uint32_t addr = abase + k * (uint32_t)sizeof(float4);
 #pragma unroll
                   for (int h = 0; h < H; ++h) {
-                     const ulonglong2 p = lds128_pairs(addr + (uint32_t)h * plane_bytes);
+                     const ulonglong2 p = lds128_pairs(addr + (uint32_t)h * stride_bytes);
                      acc2[h][r] = f2_fma(f2, p.y, f2_add(acc2[h][r], p.x));
                   }
                }
@@ -663,7 +667,7 @@ __global__ void __launch_bounds__(1024 / PPT)
                   const uint32_t addr = abase + k * (uint32_t)sizeof(float4);
 #pragma unroll
                   for (int h = 0; h < H; ++h) {
-                     const float4 p = lds128(addr + (uint32_t)h * plane_bytes);
+                     const float4 p = lds128(addr + (uint32_t)h * stride_bytes);
                      acc[2 * h][r] = fmaf(f, p.z, acc[2 * h][r] + p.x);
                      acc[2 * h + 1][r] = fmaf(f, p.w, acc[2 * h + 1][r] + p.y);
                   }
@@ -756,15 +760,18 @@ __global__ void __launch_bounds__(1024 / PPT)
    }
 }
 
+constexpr int kCPWindow = 104;  // window entries of the compile-time-stride backprojection
+
 inline size_t async_smem(int S, int ach, int wlen, int nst = 2) {
    return (size_t)nst * sizeof(float2) * (size_t)S * ach * wlen;
 }
 
-template <int S, int ACH, bool PACKED, int PPT, int NST = 2, bool CP = false>
+template <int S, int ACH, bool PACKED, int PPT, int NST = 2, bool CP = false, int WP = 0>
 cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& cfg, cudaStream_t st) {
    if (CP && (cfg.Pp > kCPAngles || !cfg.a_host || !cfg.b_host)) return cudaErrorInvalidConfiguration;
    const int wlen = window_len(cfg.scale, 32, 32);
-   const size_t smem = async_smem(S, ACH, wlen, NST);
+   if (WP > 0 && wlen > WP) return cudaErrorInvalidConfiguration;
+   const size_t smem = async_smem(S, ACH, WP > 0 ? WP : wlen, NST);
    if (smem > kMaxPairsSmem) return cudaErrorInvalidConfiguration;
    // transaction bytes armed on one mbarrier phase stay below 2^20
    if ((size_t)ACH * wlen * sizeof(float2) * S >= (1u << 20)) return cudaErrorInvalidConfiguration;
@@ -779,7 +786,7 @@ cudaError_t launch_async(const float* sino, float* img, int batch, const BPCfg& 
       if (e != cudaSuccess) return e;
    }
    if (cfg.mid_event && (e = cudaEventRecord(cfg.mid_event, st)) != cudaSuccess) return e;
-   auto kern = bp_linear_async<S, ACH, PACKED, PPT, NST, CP>;
+   auto kern = bp_linear_async<S, ACH, PACKED, PPT, NST, CP, WP>;
    if (smem > 48 * 1024) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
@@ -1105,6 +1112,10 @@ cudaError_t launch_backprojection(const float* sino, float* img, int batch, cons
    if (v.kind == kAsync || v.kind == kAsyncPacked) {
       const bool pk = v.kind == kAsyncPacked;
       const int ach = v.achunk;
+      // windows of up to kCPWindow entries (2 bins per pixel and less): a
+      // compile-time window stride
+      if (v.cp && v.slices == 4 && ach == 8 && window_len(cfg.scale, 32, 32) <= kCPWindow)
+         return launch_async<4, 8, false, 4, 2, true, kCPWindow>(sino, img, batch, cfg, st);
       if (v.cp)
          return v.slices == 2 ? launch_async_fit<2, false, 4, true>(sino, img, batch, cfg, ach, st)
                               : launch_async_fit<4, false, 4, true>(sino, img, batch, cfg, ach, st);
