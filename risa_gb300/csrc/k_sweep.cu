@@ -23,6 +23,7 @@ namespace {
 using namespace fft;
 
 constexpr int kNT = 256;
+constexpr int kSweepWarps = kNT / 32;
 constexpr float kSweepMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kSweepMagicBits = 0x4B400000;
 constexpr float kAttClamp = 1e-5f;          // the reference's `temp` (Attenuation.cu:144)
@@ -169,21 +170,24 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
       __syncthreads();
       if (!S.ok) return false;
       // the rows were written by generic-proxy stores of other CTAs; the bulk
-      // copies below read them through the async proxy
-      if (warp == 0) asm volatile("fence.proxy.async.global;" ::: "memory");
+      // copies below (issued by every warp) read them through the async proxy
+      asm volatile("fence.proxy.async.global;" ::: "memory");
       const float2* prow = A.pairs + I.pair_off;
       const uint32_t win_bytes = (uint32_t)W * (uint32_t)sizeof(float2);
       const int ACH = A.ach;
       const int nchunks = (Pp + ACH - 1) / ACH;
-      // With the host's window table, warp 0 fetches the table entries of
-      // chunk ch + 3 by cp.async while the CTA works on chunk ch + 1, so the
-      // refill after a chunk's barrier reads them from shared memory instead
-      // of waiting on global loads that every other warp would wait for at
-      // the next barrier.
+      // Every warp refills its share of a chunk: warp w's lanes 0 .. ACH/8 - 1
+      // take angles w ACH/8 + lane, and each warp arrives once on the stage's
+      // mbarrier (initialised for all the CTA's warps) with its own byte
+      // count, so no warp carries the whole refill between two CTA barriers.
+      // With the host's window table each warp fetches its entries of chunk
+      // ch + 3 by cp.async while the CTA works on chunk ch + 1, so the refill
+      // after a chunk's barrier reads them from shared memory.
       const bool pre = I.tile_win != nullptr;
+      const int apw = ACH / kSweepWarps, l = warp * apw + lane;  // this lane's angle slot
       auto prefetch = [&](int ch) {
          const int na = min(ACH, Pp - ch * ACH), s = ch & 1;
-         for (int l = lane; l < na; l += 32) {
+         if (lane < apw && l < na) {
             const int ang = ch * ACH + l;
             async::cp_async<4>(&S.pre_a[s][l], I.a + ang);
             async::cp_async<4>(&S.pre_b[s][l], I.b + ang);
@@ -193,10 +197,11 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
       };
       auto issue = [&](int ch, int st, bool from_pre) {
          const int na = min(ACH, Pp - ch * ACH);
+         const int mine = min(max(na - warp * apw, 0), apw);  // angles of this warp in the chunk
          if (from_pre) async::cp_async_wait_all();
-         if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)na * win_bytes);
+         if (lane == 0) async::mbar_arrive_expect_tx(&full[st], (uint32_t)mine * win_bytes);
          __syncwarp();
-         for (int l = lane; l < na; l += 32) {  // a lane per angle of the chunk
+         if (lane < mine) {  // a lane per angle of the warp's share
             const int ang = ch * ACH + l;
             float a, b, rel;
             int w0;
@@ -233,11 +238,9 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
                              win_bytes, &full[st]);
          }
       };
-      if (warp == 0) {
-         issue(0, 0, false);
-         if (nchunks > 1) issue(1, 1, false);
-         if (pre && nchunks > 2) prefetch(2);
-      }
+      issue(0, 0, false);
+      if (nchunks > 1) issue(1, 1, false);
+      if (pre && nchunks > 2) prefetch(2);
       __syncthreads();
 
       float acc[PPT];
@@ -301,11 +304,11 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
             if (threadIdx.x == 0) {  // the copies of the next chunk may still be in flight
                if (ch + 1 < nchunks) async::mbar_wait_quiet(&full[st ^ 1], uses[st ^ 1] & 1u);
             }
-            if (warp == 0) async::cp_async_wait_all();  // and a prefetch of table entries
+            async::cp_async_wait_all();  // and every warp's prefetch of table entries
             failed = true;
             break;
          }
-         if (warp == 0 && ch + 2 < nchunks) {
+         if (ch + 2 < nchunks) {
             issue(ch + 2, st, pre);
             if (pre && ch + 3 < nchunks) prefetch(ch + 3);
          }
@@ -339,9 +342,9 @@ __global__ void __launch_bounds__(kNT, 2) sweep_persistent(SweepArgs A) {
    __shared__ uint64_t full[2];
    __shared__ TileShared ts;
    __shared__ int s_item;
-   if (threadIdx.x == 0) {
-      async::mbar_init(&full[0], 1);
-      async::mbar_init(&full[1], 1);
+   if (threadIdx.x == 0) {  // one arrival per warp and phase (each warp refills its share)
+      async::mbar_init(&full[0], kSweepWarps);
+      async::mbar_init(&full[1], kSweepWarps);
       async::mbar_init_fence();
       atomicMin(A.t_launch, global_ns());
    }
