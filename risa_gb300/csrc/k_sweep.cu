@@ -271,7 +271,7 @@ __device__ __forceinline__ bool sweep_tile(const SweepArgs& A, const SweepInst& 
          if (!async::mbar_wait(&full[st], uses[st] & 1u, A.err, 5)) S.fail = 1;
          ++uses[st];
          const int na = live ? min(ACH, Pp - ch * ACH) : 0;
-#pragma unroll 4
+#pragma unroll 8
          for (int ai = 0; ai < na; ++ai) {
             const float4 q = S.par[st][ai];  // one broadcast load per angle
             const float a = q.x, b = q.y;
